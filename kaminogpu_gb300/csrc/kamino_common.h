@@ -1,0 +1,71 @@
+// kamino_common.h — shared host/device declarations of the GB300 solver.
+#pragma once
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include <vector_types.h>
+
+#include "../../include/kamino_gb300.h"
+
+// Records a formatted message as the thread's last error and returns code.
+int kamino_fail(int code, const char* fmt, ...)
+#if defined(__GNUC__)
+    __attribute__((format(printf, 2, 3)))
+#endif
+    ;
+
+#define KAMINO_PI_D 3.14159265358979323846   /* M_PI  (KaminoHeader.cuh:26) */
+#define KAMINO_2PI_D 6.28318530717958647692  /* M_2PI (KaminoHeader.cuh:27) */
+
+// Per-sphere constants, passed to kernels by value.  They replace the
+// reference's process-wide __constant__ parameters (KaminoCore.cu:5-9).
+struct KGeo {
+    int nt;       // nTheta (power of two)
+    int np;       // nPhi = 2 * nTheta
+    int mask;     // nPhi - 1
+    int half;     // nPhi / 2
+    int log2nt;
+    float h;      // gridLenGlobal = (float)(M_PI / nTheta), KaminoCore.cu:849
+    float halfh;  // 0.5f * h (exact)
+    float invh;   // (float)(1.0 / h), the invGridLen of the samplers
+    float R;      // radiusGlobal
+    float dt;     // timeStepGlobal
+    float cofTheta;     // dt / R (float division, KaminoCore.cu:204)
+    float pi_up;        // smallest float > M_PI: theta > M_PI  <=>  theta >= pi_up
+    float wrap_phi_hi;  // smallest float x with floorf((float)(x / M_2PI)) >= 1
+    int pitch;          // floats per row (== np)
+    int rows;           // rows allocated per field (nt + 2; the last rows read as 0)
+    uint32_t flags;     // kamino_flags
+};
+
+// Device arrays of one sphere.  Each field is [rows][pitch] floats.
+struct KBufs {
+    float* u[2];
+    float* v[2];
+    float* rho[2];
+    float2* part[2];
+    float* cu;       // geometric scratch: u at cell centres
+    float* cv;       // geometric scratch: v at cell centres
+    float* p;        // pressure
+    float2* spec;    // spectrum, [mode m-1][row], m = 1..nt
+    // per-row tables
+    float* cof_c;    // dt / (R sinf((j+1/2)h))   (centred rows, u_phi rows)
+    float* cof_v;    // dt / (R sinf((j+1)h))     (u_theta rows)
+    float* gfac;     // G = dt cosf(theta) / (R sinf(theta)) at (j+1/2)h
+    float* negHs;    // -h * sinf((j+1/2)h)
+    float* divf;     // (1/sinf(theta_j)) / h
+    float* sinN;     // sinf(theta_j - h/2)
+    float* sinS;     // sinf(theta_j + h/2)
+    float* lapA;     // Laplacian rows (FP32): A_i, C_i, B0_i, 1/sin^2
+    float* lapC;
+    float* lapB0;
+    float* lapS;
+    double* lapA64;  // same in FP64
+    double* lapC64;
+    double* lapB064;
+    double* lapS64;
+    float2* tw;      // e^{-2 pi i k / nt}, k < nt/2
+    float2* rt;      // e^{-i pi m / nt},  m <= nt
+    int64_t npart;
+};

@@ -1,0 +1,236 @@
+// kamino_device.cuh — device building blocks of the GB300 Kamino step.
+//
+// Index exactness.  The reference evaluates its sample positions with float
+// variables and double literals (KaminoHeader.cuh:26-41), so validateCoord
+// (KaminoCore.cu:11-29) and the staggering shifts run in double and round
+// to float on assignment.  Doubles are 1/64-rate on GB300, so the samplers
+// here run the common case in FP32 and reproduce the reference bit for bit:
+//  * shift: (float)((double)a - (double)h * off) equals the FP32 a - h*off
+//    because off*h is exact and one double operation followed by rounding to
+//    float equals the correctly rounded float operation (53 >= 2*24 + 2,
+//    the innocuous double-rounding bound for + - * /);
+//  * validateCoord leaves (phi, theta) untouched exactly when
+//    0 <= theta < pi_up (theta <= M_PI as a double, so no flip and the
+//    2pi-wrap count is 0) and 0 <= phi < wrap_phi_hi (the first float whose
+//    floorf((float)(phi / M_2PI)) is 1); -0.0 passes, as in the reference.
+// Everything else (pole crossings and the phi = 0 seam) goes to
+// ref_validate(), the reference's arithmetic in FP64, which only a few
+// points per row reach.  kamino_probe_index() exposes this stage so the
+// tests compare it with the reference restatement on arbitrary inputs.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "kamino_common.h"
+
+namespace kdev {
+
+// validateCoord with the reference's exact arithmetic (KaminoCore.cu:11-29).
+__device__ __noinline__ float ref_validate(float& phi, float& theta)
+{
+    float ret = 1.0f;
+    {
+        float q = __double2float_rn(__ddiv_rn((double)theta, KAMINO_2PI_D));
+        int n = (int)floorf(q);
+        theta = __double2float_rn(__dadd_rn((double)theta, -__dmul_rn((double)n, KAMINO_2PI_D)));
+    }
+    if ((double)theta > KAMINO_PI_D) {
+        theta = __double2float_rn(__dsub_rn(KAMINO_2PI_D, (double)theta));
+        phi = __double2float_rn(__dadd_rn((double)phi, KAMINO_PI_D));
+        ret = -ret;
+    }
+    if (theta < 0) {
+        theta = -theta;
+        phi = __double2float_rn(__dadd_rn((double)phi, KAMINO_PI_D));
+        ret = -ret;
+    }
+    {
+        float q = __double2float_rn(__ddiv_rn((double)phi, KAMINO_2PI_D));
+        int n = (int)floorf(q);
+        phi = __double2float_rn(__dadd_rn((double)phi, -__dmul_rn((double)n, KAMINO_2PI_D)));
+    }
+    return ret;
+}
+
+// validateCoord: FP32 fast path when no wrap applies, exact path otherwise.
+__device__ __forceinline__ bool wrap_coord(float& phi, float& theta, const KGeo& g)
+{
+    if (theta >= 0.0f && theta < g.pi_up && phi >= 0.0f && phi < g.wrap_phi_hi) return false;
+    return ref_validate(phi, theta) < 0.0f;
+}
+
+// kaminoLerp (KaminoCore.cu:31-34): (1 - t) a + t b.
+__device__ __forceinline__ float klerp(float a, float b, float t)
+{
+    return __fmaf_rn(t, b, __fmul_rn(1.0f - t, a));
+}
+
+enum { KIND_VPHI = 0, KIND_VTHETA = 1, KIND_CENTERED = 2 };
+
+struct SampleIndex {
+    int ip, it;      // phiIndex (wrapped to [0, nPhi)), thetaIndex
+    float ap, at;    // alphaPhi, alphaTheta
+    bool flipped;    // validateCoord returned -1
+    bool pole;       // the pole branch of the sampler
+};
+
+// Index stage of sampleVPhi / sampleVTheta / sampleCentered
+// (KaminoCore.cu:38-52, 88-103, 138-153).
+template <int KIND>
+__device__ __forceinline__ SampleIndex sample_index(float phiRaw, float thetaRaw, const KGeo& g)
+{
+    // staggering offsets: u_phi (-0.5, 0.5), u_theta (0, 1), centred (0, 0.5)
+    float phi = (KIND == KIND_VPHI) ? __fadd_rn(phiRaw, g.halfh) : phiRaw;
+    float theta = (KIND == KIND_VTHETA) ? __fsub_rn(thetaRaw, g.h) : __fsub_rn(thetaRaw, g.halfh);
+    SampleIndex s;
+    s.flipped = wrap_coord(phi, theta, g);
+    float nphi = __fmul_rn(phi, g.invh), nth = __fmul_rn(theta, g.invh);
+    float fp = floorf(nphi), ft = floorf(nth);
+    s.ap = __fsub_rn(nphi, fp);
+    s.at = __fsub_rn(nth, ft);
+    s.ip = ((int)fp) & g.mask;
+    // After validateCoord theta is in [0, pi], so thetaIndex is in [0, nt].
+    // The clamp only matters for non-finite input, where it keeps every read
+    // inside the allocation instead of faulting.
+    s.it = min(max((int)ft, 0), g.nt);
+    const int pole_row = (KIND == KIND_VTHETA) ? g.nt - 2 : g.nt - 1;
+    s.pole = (s.it == 0 && s.flipped) || s.it == pole_row;
+    return s;
+}
+
+// Bilinear sample with the reference's pole branch.  vec selects the
+// optional sign flip of vector components across a pole.
+template <int KIND>
+__device__ __forceinline__ float sample(const float* __restrict__ f, float phiRaw, float thetaRaw,
+                                        const KGeo& g, bool vec_flip)
+{
+    SampleIndex s = sample_index<KIND>(phiRaw, thetaRaw, g);
+    const int i0 = s.ip, i1 = (s.ip + 1) & g.mask;
+    const float* r0 = f + (size_t)s.it * g.pitch;
+    float v00 = __ldg(r0 + i0), v01 = __ldg(r0 + i1);
+    if (s.pole) {
+        const int j0 = (i0 + g.half) & g.mask, j1 = (i1 + g.half) & g.mask;
+        float v10 = __ldg(r0 + j0), v11 = __ldg(r0 + j1);
+        float lo = klerp(v00, v01, s.ap), hi = klerp(v10, v11, s.ap);
+        if (vec_flip) hi = -hi;
+        float w = (KIND == KIND_VPHI) ? s.at : 0.5f * s.at;
+        float r = klerp(lo, hi, w);
+        return (vec_flip && s.flipped) ? -r : r;
+    }
+    const float* r1 = r0 + g.pitch;
+    float v10 = __ldg(r1 + i0), v11 = __ldg(r1 + i1);
+    float r = klerp(klerp(v00, v01, s.ap), klerp(v10, v11, s.ap), s.at);
+    return (vec_flip && s.flipped) ? -r : r;
+}
+
+// RK2 back-trace of one grid point (advectionVPhiKernel /
+// advectionVThetaKernel / advectionCentered, KaminoCore.cu:186-319).
+// cofPhi = dt / (R sinf(gTheta)) comes from a per-row table computed with
+// the same expression.
+template <int KIND>
+__device__ __forceinline__ float advect_point(const float* __restrict__ u, const float* __restrict__ v,
+                                              const float* __restrict__ field, float gPhi, float gTheta,
+                                              float cofPhi, const KGeo& g)
+{
+    const bool vf = (g.flags & KAMINO_F_POLE_SIGN_FLIP) != 0;
+    float guPhi = sample<KIND_VPHI>(u, gPhi, gTheta, g, vf);
+    float guTheta = sample<KIND_VTHETA>(v, gPhi, gTheta, g, vf);
+    float deltaPhi = __fmul_rn(guPhi, cofPhi);
+    float deltaTheta = __fmul_rn(guTheta, g.cofTheta);
+    float midPhi = __fsub_rn(gPhi, 0.5f * deltaPhi);
+    float midTheta = __fsub_rn(gTheta, 0.5f * deltaTheta);
+    float muPhi = sample<KIND_VPHI>(u, midPhi, midTheta, g, vf);
+    float muTheta = sample<KIND_VTHETA>(v, midPhi, midTheta, g, vf);
+    float averuPhi = 0.5f * __fadd_rn(muPhi, guPhi);
+    float averuTheta = 0.5f * __fadd_rn(muTheta, guTheta);
+    deltaPhi = __fmul_rn(averuPhi, cofPhi);
+    deltaTheta = __fmul_rn(averuTheta, g.cofTheta);
+    float pPhi = __fsub_rn(gPhi, deltaPhi);
+    float pTheta = __fsub_rn(gTheta, deltaTheta);
+    return sample<KIND>(field, pPhi, pTheta, g, vf && KIND != KIND_CENTERED);
+}
+
+// ------------------------------------------------------------ geometric
+// The reference's solveCubic (KaminoCore.cu:421-454) with a = 0, in FP64,
+// used only when 1 + G v <= 0 (three real roots possible).
+__device__ __noinline__ double ref_solve_cubic64(double b, double c)
+{
+    const double eps = (double)1e-7f;
+    double q = (0.0 - 3 * b) / 9.0;
+    double r = (27.0 * c) / 54.0;
+    double r2 = r * r, q3 = q * q * q;
+    if (r2 <= (q3 + eps)) {
+        double t = r / sqrt(q3);
+        if (t < -1) t = -1;
+        if (t > 1) t = 1;
+        t = acos(t);
+        q = -2.0 * sqrt(q);
+        return q * cos(t / 3.0);
+    }
+    double x = fabs(r) + sqrt(r2 - q3);
+    double A = (x > 0 && isfinite(x)) ? -cbrt(x) : -x;
+    if (r < 0) A = -A;
+    double B = A == 0 ? 0 : q / A;
+    return A + B;
+}
+
+// u' of geometricFillKernel (KaminoCore.cu:494-508): the root the reference
+// takes of u^3 + ((G v + 1)/G^2) u - uPrev/G^2 = 0.  When 1 + G v > 0 that
+// root is unique and g(u) = G^2 u^3 + (1 + G v) u - uPrev is increasing and
+// convex/concave on either side of 0, so Newton from uPrev/(1 + G v)
+// converges monotonically; FP32 keeps full relative accuracy (the
+// reference's FP32 Cardano form cancels A + B catastrophically near the
+// equator, where G is small).
+__device__ __forceinline__ float geo_root(float G, float uPrev, float vPrev)
+{
+    if (!(fabsf(G) > 1e-7f)) return uPrev;
+    float a = __fmaf_rn(G, vPrev, 1.0f);
+    if (a > 0.0f) {
+        float G2 = G * G;
+        float x = uPrev / a;
+        for (int k = 0; k < 40; k++) {
+            float x2 = x * x;
+            float f = __fmaf_rn(G2 * x2, x, __fmaf_rn(a, x, -uPrev));
+            float df = __fmaf_rn(3.0f * G2, x2, a);
+            float dx = f / df;
+            x -= dx;
+            if (!(fabsf(dx) > 5e-7f * fabsf(x))) break;
+        }
+        return x;
+    }
+    double G2 = (double)G * (double)G;
+    return (float)ref_solve_cubic64(((double)G * vPrev + 1.0) / G2, -(double)uPrev / G2);
+}
+
+// ---------------------------------------------------------------- FFT
+// Radix-2 complex FFT of length n (power of two) on one row in shared memory,
+// worked by one warp.  dit(): bit-reversed input, natural output.
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(__fmaf_rn(a.x, b.x, -a.y * b.y), __fmaf_rn(a.x, b.y, a.y * b.x));
+}
+
+template <bool INVERSE>
+__device__ __forceinline__ void fft_dit_warp(float2* x, int n, int log2n, const float2* __restrict__ tw,
+                                             int lane)
+{
+    for (int s = 1; s <= log2n; s++) {
+        const int half = 1 << (s - 1);
+        const int tstep = n >> s;
+        for (int b = lane; b < (n >> 1); b += 32) {
+            const int grp = b >> (s - 1), k = b & (half - 1);
+            const int i = (grp << s) + k, j = i + half;
+            float2 w = __ldg(tw + k * tstep);
+            if (INVERSE) w.y = -w.y;
+            float2 t = cmul(w, x[j]);
+            float2 a = x[i];
+            x[i] = make_float2(a.x + t.x, a.y + t.y);
+            x[j] = make_float2(a.x - t.x, a.y - t.y);
+        }
+        __syncwarp();
+    }
+}
+
+__device__ __forceinline__ int bitrev(int k, int log2n) { return (int)(__brev((unsigned)k) >> (32 - log2n)); }
+
+} // namespace kdev

@@ -1,0 +1,795 @@
+// kamino_solver.cu — one-sphere solver behind the C ABI (kamino_gb300.h).
+//
+// Host orchestration replacing KaminoSolver (KaminoGPU/kernel/KaminoSolver.cu
+// :12-238) and the stage functions of KaminoCore.cu (:344-384, 551-583,
+// 749-842).  All state lives in one device arena allocated at create time;
+// a step is five kernel launches (kamino_kernels.cuh) replayed from a CUDA
+// graph on the handle's own stream.  Every failure returns a status code.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "kamino_common.h"
+#include "kamino_kernels.cuh"
+
+// ------------------------------------------------------------------ errors
+static thread_local char g_err[1024] = "";
+
+int kamino_fail(int code, const char* fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+extern "C" const char* kamino_last_error(void) { return g_err; }
+
+#define KCUDA(call)                                                                                  \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess)                                                                       \
+            return kamino_fail(KAMINO_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                               __FILE__, __LINE__);                                                  \
+    } while (0)
+
+// ------------------------------------------------------------------ handle
+struct kamino_solver_s {
+    kamino_config cfg;
+    KGeo g;
+    KBufs b;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    int cur_uv = 0, cur_r = 0;  // which buffer holds (u, v) and (thickness, particles)
+    int nfp64 = 0;
+    int64_t steps = 0;
+    double time = 0.0;
+    float last_dt = 0.0f;
+    cudaGraphExec_t graph[2][2][2] = {};  // [steps-1][cur_uv][cur_r]
+    void* flush = nullptr;
+    size_t flush_bytes = 0;
+    size_t smem_div = 0, smem_solve = 0, smem_ifft = 0;
+};
+
+static const char* const kKernelNames[] = {"k_advect", "k_geo_centers", "k_div_fft", "k_solve",
+                                           "k_ifft_grad"};
+static const int kNumKernels = 5;
+
+extern "C" const char* kamino_kernel_name(int index)
+{
+    return (index >= 0 && index < kNumKernels) ? kKernelNames[index] : "";
+}
+
+// Smallest float x with floorf((float)((double)x / M_2PI)) >= 1, i.e. the
+// first phi the reference wraps back by 2pi (KaminoCore.cu:27).
+static float wrap_threshold()
+{
+    auto wraps = [](float x) { return (int)floorf((float)((double)x / KAMINO_2PI_D)) >= 1; };
+    float x = (float)KAMINO_2PI_D;
+    while (wraps(x)) x = nextafterf(x, 0.0f);
+    while (!wraps(x)) x = nextafterf(x, 100.0f);
+    return x;
+}
+
+static float pi_up_threshold()
+{
+    // smallest float strictly greater than M_PI (as a double)
+    float x = (float)KAMINO_PI_D;
+    while ((double)x > KAMINO_PI_D) x = nextafterf(x, 0.0f);
+    while (!((double)x > KAMINO_PI_D)) x = nextafterf(x, 100.0f);
+    return x;
+}
+
+static int fill_geo(const kamino_config* c, KGeo* g)
+{
+    const int nt = c->n_theta;
+    if (nt < 16 || nt > 2048 || (nt & (nt - 1)))
+        return kamino_fail(KAMINO_ERR_INVALID, "n_theta=%d: must be a power of two in [16, 2048]", nt);
+    if (!(c->radius > 0) || !std::isfinite(c->radius))
+        return kamino_fail(KAMINO_ERR_INVALID, "radius=%g must be positive", c->radius);
+    if (!(c->dt > 0) || !std::isfinite(c->dt))
+        return kamino_fail(KAMINO_ERR_INVALID, "dt=%g must be positive", c->dt);
+    std::memset(g, 0, sizeof(*g));
+    g->nt = nt;
+    g->np = 2 * nt;
+    g->mask = g->np - 1;
+    g->half = nt;
+    int l = 0;
+    while ((1 << l) < nt) l++;
+    g->log2nt = l;
+    g->h = (float)(KAMINO_PI_D / nt);  // Kamino::gridLen, KaminoCore.cu:849
+    g->halfh = 0.5f * g->h;
+    g->invh = (float)(1.0 / (double)g->h);
+    g->R = (float)c->radius;
+    g->dt = (float)c->dt;
+    g->cofTheta = g->dt / g->R;
+    g->pi_up = pi_up_threshold();
+    g->wrap_phi_hi = wrap_threshold();
+    g->pitch = g->np;
+    g->rows = nt + 2;
+    g->flags = c->flags;
+    return KAMINO_OK;
+}
+
+static size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static void destroy_graphs(kamino_solver_s* h)
+{
+    for (auto& a : h->graph)
+        for (auto& b : a)
+            for (auto& e : b)
+                if (e) {
+                    cudaGraphExecDestroy(e);
+                    e = nullptr;
+                }
+}
+
+extern "C" int kamino_destroy(kamino_handle h)
+{
+    if (!h) return KAMINO_OK;
+    int dev0 = 0;
+    cudaGetDevice(&dev0);
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    destroy_graphs(h);
+    if (h->arena) cudaFree(h->arena);
+    if (h->flush) cudaFree(h->flush);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    cudaSetDevice(dev0);
+    delete h;
+    return KAMINO_OK;
+}
+
+// Laplacian rows of precomputeABCKernel (KaminoSolver.cu:128-159) for n != 0,
+// with h = pi/nTheta in double: B(n) = B0 - n^2 * S.
+static void laplacian_rows(int nt, std::vector<double>& A, std::vector<double>& C, std::vector<double>& B0,
+                           std::vector<double>& S)
+{
+    const double h = KAMINO_PI_D / nt;
+    A.resize(nt);
+    C.resize(nt);
+    B0.resize(nt);
+    S.resize(nt);
+    for (int i = 0; i < nt; i++) {
+        double th = (i + 0.5) * h, c = std::cos(th), s = std::sin(th);
+        double a = 1.0 / (h * h) - c / 2.0 / h / s;
+        double cc = 1.0 / (h * h) + c / 2.0 / h / s;
+        double b0 = -2.0 / (h * h);
+        if (i == 0) {
+            b0 += a;
+            a = 0.0;
+        }
+        if (i == nt - 1) {
+            b0 += cc;
+            cc = 0.0;
+        }
+        A[i] = a;
+        C[i] = cc;
+        B0[i] = b0;
+        S[i] = 1.0 / (s * s);
+    }
+}
+
+extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
+{
+    if (!cfg || !out) return kamino_fail(KAMINO_ERR_INVALID, "kamino_create: null argument");
+    *out = nullptr;
+    KGeo g;
+    int rc = fill_geo(cfg, &g);
+    if (rc) return rc;
+    int64_t npart = kamino_particle_count(cfg);
+    if (npart < 0 || npart > ((int64_t)1 << 31))
+        return kamino_fail(KAMINO_ERR_INVALID, "particle count %lld out of range", (long long)npart);
+    if (cfg->fp64_modes < 0) return kamino_fail(KAMINO_ERR_INVALID, "fp64_modes must be >= 0");
+    int ndev = 0;
+    KCUDA(cudaGetDeviceCount(&ndev));
+    if (cfg->device < 0 || cfg->device >= ndev)
+        return kamino_fail(KAMINO_ERR_INVALID, "device %d not present (%d devices)", cfg->device, ndev);
+    KCUDA(cudaSetDevice(cfg->device));
+
+    auto* h = new kamino_solver_s();
+    h->cfg = *cfg;
+    h->g = g;
+    h->device = cfg->device;
+    h->nfp64 = std::min(cfg->fp64_modes, g.nt);
+    h->last_dt = g.dt;
+    const int nt = g.nt, np = g.np;
+    const size_t field = align_up(sizeof(float) * (size_t)g.rows * np);
+    const size_t spec = align_up(sizeof(float2) * (size_t)nt * nt);
+    const size_t part = align_up(sizeof(float2) * (size_t)std::max<int64_t>(npart, 1));
+    const size_t rowf = align_up(sizeof(float) * nt), rowd = align_up(sizeof(double) * nt);
+    const size_t tw = align_up(sizeof(float2) * nt), rt = align_up(sizeof(float2) * (nt + 1));
+    size_t total = 9 * field + spec + 2 * part + 11 * rowf + 4 * rowd + tw + rt;
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&h->arena, total);
+    if (e != cudaSuccess) {
+        int code = e == cudaErrorMemoryAllocation ? KAMINO_ERR_ALLOC : KAMINO_ERR_CUDA;
+        kamino_destroy(h);
+        return kamino_fail(code, "kamino_create: %s (%zu bytes)", cudaGetErrorString(e), total);
+    }
+    h->arena_bytes = total;
+    char* p = (char*)h->arena;
+    auto take = [&p](size_t n) {
+        char* r = p;
+        p += n;
+        return r;
+    };
+    KBufs& b = h->b;
+    for (int s = 0; s < 2; s++) {
+        b.u[s] = (float*)take(field);
+        b.v[s] = (float*)take(field);
+        b.rho[s] = (float*)take(field);
+        b.part[s] = (float2*)take(part);
+    }
+    b.cu = (float*)take(field);
+    b.cv = (float*)take(field);
+    b.p = (float*)take(field);
+    b.spec = (float2*)take(spec);
+    b.cof_c = (float*)take(rowf);
+    b.cof_v = (float*)take(rowf);
+    b.gfac = (float*)take(rowf);
+    b.negHs = (float*)take(rowf);
+    b.divf = (float*)take(rowf);
+    b.sinN = (float*)take(rowf);
+    b.sinS = (float*)take(rowf);
+    b.lapA = (float*)take(rowf);
+    b.lapC = (float*)take(rowf);
+    b.lapB0 = (float*)take(rowf);
+    b.lapS = (float*)take(rowf);
+    b.lapA64 = (double*)take(rowd);
+    b.lapC64 = (double*)take(rowd);
+    b.lapB064 = (double*)take(rowd);
+    b.lapS64 = (double*)take(rowd);
+    b.tw = (float2*)take(tw);
+    b.rt = (float2*)take(rt);
+    b.npart = npart;
+
+    rc = KAMINO_OK;
+    do {
+        e = cudaMemsetAsync(h->arena, 0, total, h->stream);
+        if (e != cudaSuccess) break;
+        std::vector<double> A, C, B0, S;
+        laplacian_rows(nt, A, C, B0, S);
+        std::vector<float> Af(A.begin(), A.end()), Cf(C.begin(), C.end()), B0f(B0.begin(), B0.end()),
+            Sf(S.begin(), S.end());
+        std::vector<float2> twh(nt), rth(nt + 1);
+        for (int k = 0; k < nt; k++) {
+            double a = -2.0 * KAMINO_PI_D * k / nt;
+            twh[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+        }
+        for (int m = 0; m <= nt; m++) {
+            double a = -KAMINO_PI_D * m / nt;
+            rth[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+        }
+        struct {
+            void* d;
+            const void* s;
+            size_t n;
+        } ups[] = {{b.lapA, Af.data(), 4 * (size_t)nt},    {b.lapC, Cf.data(), 4 * (size_t)nt},
+                   {b.lapB0, B0f.data(), 4 * (size_t)nt},  {b.lapS, Sf.data(), 4 * (size_t)nt},
+                   {b.lapA64, A.data(), 8 * (size_t)nt},   {b.lapC64, C.data(), 8 * (size_t)nt},
+                   {b.lapB064, B0.data(), 8 * (size_t)nt}, {b.lapS64, S.data(), 8 * (size_t)nt},
+                   {b.tw, twh.data(), 8 * (size_t)nt},     {b.rt, rth.data(), 8 * (size_t)(nt + 1)}};
+        for (auto& u : ups) {
+            e = cudaMemcpyAsync(u.d, u.s, u.n, cudaMemcpyHostToDevice, h->stream);
+            if (e != cudaSuccess) break;
+        }
+        if (e != cudaSuccess) break;
+        kk::k_tables<<<(nt + 127) / 128, 128, 0, h->stream>>>(h->g, h->b);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) break;
+        e = cudaStreamSynchronize(h->stream);  // host vectors above go out of scope
+        if (e != cudaSuccess) break;
+        h->smem_div = sizeof(float2) * kk::FFT_ROWS * (nt + 1);
+        h->smem_solve = (size_t)kk::SOLVE_WARPS * 4 * (nt + 32) * sizeof(float);
+        h->smem_ifft = sizeof(float2) * 2 * (kk::FFT_ROWS + 1) * (nt + 1);
+        e = cudaFuncSetAttribute(kk::k_div_fft<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem_div);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(kk::k_div_fft<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)h->smem_div);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(kk::k_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)h->smem_solve);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(kk::k_ifft_grad, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)h->smem_ifft);
+    } while (0);
+    if (e != cudaSuccess) {
+        rc = kamino_fail(KAMINO_ERR_CUDA, "kamino_create: %s", cudaGetErrorString(e));
+        kamino_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return KAMINO_OK;
+}
+
+// ----------------------------------------------------------------- launches
+static int launch_advect(kamino_solver_s* h, int suv, int duv, int sr, int dr)
+{
+    const KGeo& g = h->g;
+    const int T = kk::ADV_THREADS;
+    int nb_u = (g.nt * g.np + T - 1) / T, nb_v = ((g.nt - 1) * g.np + T - 1) / T, nb_r = nb_u;
+    int nb_p = (int)((h->b.npart + T - 1) / T);
+    kk::k_advect<<<nb_u + nb_v + nb_r + nb_p, T, 0, h->stream>>>(g, h->b, suv, duv, sr, dr, nb_u, nb_v, nb_r);
+    return cudaGetLastError() == cudaSuccess ? KAMINO_OK : KAMINO_ERR_CUDA;
+}
+
+static int launch_geo(kamino_solver_s* h, int src)
+{
+    const KGeo& g = h->g;
+    int n = g.nt * g.np;
+    kk::k_geo_centers<<<(n + 255) / 256, 256, 0, h->stream>>>(g, h->b, src);
+    return cudaGetLastError() == cudaSuccess ? KAMINO_OK : KAMINO_ERR_CUDA;
+}
+
+template <int MODE>
+static int launch_div(kamino_solver_s* h, int uv_in, int uv_out)
+{
+    const KGeo& g = h->g;
+    kk::k_div_fft<MODE><<<g.nt / kk::FFT_ROWS, 32 * kk::FFT_ROWS, MODE == 1 ? 0 : h->smem_div, h->stream>>>(
+        g, h->b, uv_in, uv_out);
+    return cudaGetLastError() == cudaSuccess ? KAMINO_OK : KAMINO_ERR_CUDA;
+}
+
+static int launch_solve(kamino_solver_s* h)
+{
+    const KGeo& g = h->g;
+    int n32 = g.nt - h->nfp64;
+    int grid = h->nfp64 + (n32 + kk::SOLVE_WARPS - 1) / kk::SOLVE_WARPS;
+    kk::k_solve<<<grid, 32 * kk::SOLVE_WARPS, h->smem_solve, h->stream>>>(g, h->b, h->nfp64);
+    return cudaGetLastError() == cudaSuccess ? KAMINO_OK : KAMINO_ERR_CUDA;
+}
+
+static int launch_ifft(kamino_solver_s* h, int uv_in, int uv_out)
+{
+    const KGeo& g = h->g;
+    int wp = (g.flags & KAMINO_F_NO_PRESSURE_OUT) ? 0 : 1;
+    kk::k_ifft_grad<<<g.nt / kk::FFT_ROWS, 32 * (kk::FFT_ROWS + 1), h->smem_ifft, h->stream>>>(g, h->b, uv_in,
+                                                                                              uv_out, wp);
+    return cudaGetLastError() == cudaSuccess ? KAMINO_OK : KAMINO_ERR_CUDA;
+}
+
+// The fused step from parity (cu, cr); ev, when given, receives an external
+// event record before the first and after every kernel (6 events).
+static int enqueue_step(kamino_solver_s* h, int cu, int cr, cudaEvent_t* ev)
+{
+    int rc = 0;
+    auto mark = [&](int k) {
+        if (ev) cudaEventRecordWithFlags(ev[k], h->stream, cudaEventRecordExternal);
+    };
+    mark(0);
+    rc |= launch_advect(h, cu, 1 - cu, cr, 1 - cr);
+    mark(1);
+    rc |= launch_geo(h, 1 - cu);
+    mark(2);
+    rc |= launch_div<0>(h, 1 - cu, cu);
+    mark(3);
+    rc |= launch_solve(h);
+    mark(4);
+    rc |= launch_ifft(h, cu, 1 - cu);
+    mark(5);
+    return rc ? kamino_fail(KAMINO_ERR_CUDA, "kernel launch failed: %s",
+                            cudaGetErrorString(cudaGetLastError()))
+              : KAMINO_OK;
+}
+
+static int get_graph(kamino_solver_s* h, int nsteps, cudaGraphExec_t* out)
+{
+    cudaGraphExec_t& ge = h->graph[nsteps - 1][h->cur_uv][h->cur_r];
+    if (!ge) {
+        cudaGraph_t graph = nullptr;
+        KCUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = KAMINO_OK;
+        int cu = h->cur_uv, cr = h->cur_r;
+        for (int s = 0; s < nsteps && rc == KAMINO_OK; s++) {
+            rc = enqueue_step(h, cu, cr, nullptr);
+            cu ^= 1;
+            cr ^= 1;
+        }
+        cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+        if (rc != KAMINO_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (e != cudaSuccess) return kamino_fail(KAMINO_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&ge, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            ge = nullptr;
+            return kamino_fail(KAMINO_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+        }
+    }
+    *out = ge;
+    return KAMINO_OK;
+}
+
+static int check_handle(kamino_solver_s* h)
+{
+    if (!h) return kamino_fail(KAMINO_ERR_INVALID, "null handle");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return kamino_fail(KAMINO_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+    return KAMINO_OK;
+}
+
+// Rebuild dt-dependent tables when KAMINO_F_HONOR_STEP_DT asks for a new dt.
+static int apply_dt(kamino_solver_s* h, float dt)
+{
+    if (!(h->g.flags & KAMINO_F_HONOR_STEP_DT) || dt == h->g.dt) return KAMINO_OK;
+    if (!(dt > 0) || !std::isfinite(dt)) return kamino_fail(KAMINO_ERR_INVALID, "dt=%g must be positive", dt);
+    h->g.dt = dt;
+    h->g.cofTheta = dt / h->g.R;
+    kk::k_tables<<<(h->g.nt + 127) / 128, 128, 0, h->stream>>>(h->g, h->b);
+    KCUDA(cudaGetLastError());
+    destroy_graphs(h);
+    return KAMINO_OK;
+}
+
+extern "C" int kamino_step(kamino_handle h, float dt)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    h->last_dt = dt;  // stored, as stepForward does (KaminoSolver.cu:199)
+    rc = apply_dt(h, dt);
+    if (rc) return rc;
+    cudaGraphExec_t ge;
+    rc = get_graph(h, 1, &ge);
+    if (rc) return rc;
+    KCUDA(cudaGraphLaunch(ge, h->stream));
+    h->cur_uv ^= 1;
+    h->cur_r ^= 1;
+    h->steps++;
+    h->time += h->g.dt;
+    return KAMINO_OK;
+}
+
+extern "C" int kamino_step_n(kamino_handle h, int n)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (n < 0) return kamino_fail(KAMINO_ERR_INVALID, "step count %d < 0", n);
+    for (int k = 0; k < n;) {
+        int s = (n - k >= 2) ? 2 : 1;
+        cudaGraphExec_t ge;
+        rc = get_graph(h, s, &ge);
+        if (rc) return rc;
+        KCUDA(cudaGraphLaunch(ge, h->stream));
+        if (s == 1) {
+            h->cur_uv ^= 1;
+            h->cur_r ^= 1;
+        }
+        h->steps += s;
+        h->time += (double)h->g.dt * s;
+        k += s;
+    }
+    return KAMINO_OK;
+}
+
+extern "C" int kamino_advection(kamino_handle h)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    rc = launch_advect(h, h->cur_uv, 1 - h->cur_uv, h->cur_r, 1 - h->cur_r);
+    if (rc) return kamino_fail(rc, "k_advect launch: %s", cudaGetErrorString(cudaGetLastError()));
+    h->cur_uv ^= 1;
+    h->cur_r ^= 1;
+    return KAMINO_OK;
+}
+
+extern "C" int kamino_geometric(kamino_handle h)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    rc = launch_geo(h, h->cur_uv);
+    if (!rc) rc = launch_div<1>(h, h->cur_uv, 1 - h->cur_uv);
+    if (rc) return kamino_fail(rc, "geometric launch: %s", cudaGetErrorString(cudaGetLastError()));
+    h->cur_uv ^= 1;
+    return KAMINO_OK;
+}
+
+extern "C" int kamino_projection(kamino_handle h)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    rc = launch_div<2>(h, h->cur_uv, 1 - h->cur_uv);
+    if (!rc) rc = launch_solve(h);
+    if (!rc) rc = launch_ifft(h, h->cur_uv, 1 - h->cur_uv);
+    if (rc) return kamino_fail(rc, "projection launch: %s", cudaGetErrorString(cudaGetLastError()));
+    h->cur_uv ^= 1;
+    h->steps++;  // a full advection+geometric+projection sequence is a step
+    h->time += h->g.dt;
+    return KAMINO_OK;
+}
+
+extern "C" int kamino_run_frames(kamino_handle h, int frames, int64_t* steps_taken)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (frames < 0) return kamino_fail(KAMINO_ERR_INVALID, "frames=%d < 0", frames);
+    int64_t total = kamino_frame_steps(h->cfg.dt, h->cfg.frame_dt, frames);
+    if (total < 0) return kamino_fail(KAMINO_ERR_INVALID, "frame_dt and dt must be > 0");
+    if (total > 0x7fffffff) return kamino_fail(KAMINO_ERR_INVALID, "too many steps");
+    rc = kamino_step_n(h, (int)total);
+    if (steps_taken) *steps_taken = total;
+    return rc;
+}
+
+extern "C" int kamino_synchronize(kamino_handle h)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    KCUDA(cudaStreamSynchronize(h->stream));
+    return KAMINO_OK;
+}
+
+extern "C" int kamino_time_elapsed(kamino_handle h, double* t, int64_t* steps)
+{
+    if (!h) return kamino_fail(KAMINO_ERR_INVALID, "null handle");
+    if (t) *t = h->time;
+    if (steps) *steps = h->steps;
+    return KAMINO_OK;
+}
+
+extern "C" int kamino_launches_per_step(kamino_handle) { return kNumKernels; }
+
+extern "C" int kamino_device_bytes(kamino_handle h, size_t* bytes)
+{
+    if (!h || !bytes) return kamino_fail(KAMINO_ERR_INVALID, "null argument");
+    *bytes = h->arena_bytes;
+    return KAMINO_OK;
+}
+
+// --------------------------------------------------------------- state I/O
+static int field_geometry(kamino_solver_s* h, int field, int* rows)
+{
+    switch (field) {
+    case KAMINO_U_PHI:
+    case KAMINO_THICKNESS:
+    case KAMINO_PRESSURE: *rows = h->g.nt; return KAMINO_OK;
+    case KAMINO_U_THETA: *rows = h->g.nt - 1; return KAMINO_OK;
+    case KAMINO_PARTICLES: *rows = 0; return KAMINO_OK;
+    }
+    return kamino_fail(KAMINO_ERR_INVALID, "unknown field %d", field);
+}
+
+static float* field_dev(kamino_solver_s* h, int field)
+{
+    switch (field) {
+    case KAMINO_U_PHI: return h->b.u[h->cur_uv];
+    case KAMINO_U_THETA: return h->b.v[h->cur_uv];
+    case KAMINO_THICKNESS: return h->b.rho[h->cur_r];
+    case KAMINO_PRESSURE: return h->b.p;
+    case KAMINO_PARTICLES: return (float*)h->b.part[h->cur_r];
+    }
+    return nullptr;
+}
+
+static int copy_field(kamino_solver_s* h, int field, void* other, size_t pitch, bool to_device,
+                      cudaMemcpyKind kind, bool sync)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!other) return kamino_fail(KAMINO_ERR_INVALID, "null buffer");
+    int rows;
+    rc = field_geometry(h, field, &rows);
+    if (rc) return rc;
+    float* d = field_dev(h, field);
+    if (field == KAMINO_PARTICLES) {
+        size_t n = sizeof(float2) * (size_t)h->b.npart;
+        if (n == 0) return KAMINO_OK;
+        if (to_device)
+            KCUDA(cudaMemcpyAsync(d, other, n, kind, h->stream));
+        else
+            KCUDA(cudaMemcpyAsync(other, d, n, kind, h->stream));
+    } else {
+        const size_t w = sizeof(float) * h->g.np;
+        if (pitch == 0) pitch = w;
+        if (pitch < w) return kamino_fail(KAMINO_ERR_INVALID, "pitch %zu < row bytes %zu", pitch, w);
+        if (to_device)
+            KCUDA(cudaMemcpy2DAsync(d, w, other, pitch, w, rows, kind, h->stream));
+        else
+            KCUDA(cudaMemcpy2DAsync(other, pitch, d, w, w, rows, kind, h->stream));
+    }
+    if (sync) KCUDA(cudaStreamSynchronize(h->stream));
+    return KAMINO_OK;
+}
+
+extern "C" int kamino_set_state(kamino_handle h, int field, const float* host, size_t pitch_bytes)
+{
+    return copy_field(h, field, (void*)host, pitch_bytes, true, cudaMemcpyHostToDevice, true);
+}
+
+extern "C" int kamino_get_state(kamino_handle h, int field, float* host, size_t pitch_bytes)
+{
+    return copy_field(h, field, host, pitch_bytes, false, cudaMemcpyDeviceToHost, true);
+}
+
+extern "C" int kamino_set_state_device(kamino_handle h, int field, const float* dev, size_t pitch_bytes)
+{
+    return copy_field(h, field, (void*)dev, pitch_bytes, true, cudaMemcpyDeviceToDevice, false);
+}
+
+extern "C" int kamino_get_state_device(kamino_handle h, int field, float* dev, size_t pitch_bytes)
+{
+    return copy_field(h, field, dev, pitch_bytes, false, cudaMemcpyDeviceToDevice, false);
+}
+
+// ----------------------------------------------------------------- timing
+static int ensure_flush(kamino_solver_s* h)
+{
+    if (h->flush) return KAMINO_OK;
+    // larger than the 129 MB L2 of GB300
+    h->flush_bytes = (size_t)256 << 20;
+    cudaError_t e = cudaMalloc(&h->flush, h->flush_bytes);
+    if (e != cudaSuccess) {
+        h->flush = nullptr;
+        return kamino_fail(KAMINO_ERR_ALLOC, "L2 flush buffer: %s", cudaGetErrorString(e));
+    }
+    return KAMINO_OK;
+}
+
+extern "C" int kamino_time_steps(kamino_handle h, int n, int flush_l2, double* ms_total)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (n <= 0 || !ms_total) return kamino_fail(KAMINO_ERR_INVALID, "bad arguments");
+    if (flush_l2 && (rc = ensure_flush(h))) return rc;
+    std::vector<cudaEvent_t> ev(2 * (size_t)n, nullptr);
+    for (auto& e : ev) KCUDA(cudaEventCreate(&e));
+    for (int k = 0; k < n && rc == KAMINO_OK; k++) {
+        if (flush_l2) KCUDA(cudaMemsetAsync(h->flush, k & 0xff, h->flush_bytes, h->stream));
+        KCUDA(cudaEventRecord(ev[2 * k], h->stream));
+        rc = kamino_step(h, h->g.dt);
+        KCUDA(cudaEventRecord(ev[2 * k + 1], h->stream));
+    }
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    double tot = 0;
+    for (int k = 0; k < n && e == cudaSuccess; k++) {
+        float ms = 0;
+        e = cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]);
+        tot += ms;
+    }
+    for (auto& x : ev) cudaEventDestroy(x);
+    if (rc) return rc;
+    if (e != cudaSuccess) return kamino_fail(KAMINO_ERR_CUDA, "timing: %s", cudaGetErrorString(e));
+    *ms_total = tot;
+    return KAMINO_OK;
+}
+
+extern "C" int kamino_time_kernels(kamino_handle h, int reps, int flush_l2, double* ms, int max, int* count)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (reps <= 0 || !ms) return kamino_fail(KAMINO_ERR_INVALID, "bad arguments");
+    if (flush_l2 && (rc = ensure_flush(h))) return rc;
+    std::vector<double> acc(kNumKernels, 0.0);
+    cudaEvent_t ev[2][6];
+    for (auto& row : ev)
+        for (auto& e : row) KCUDA(cudaEventCreate(&e));
+    // one graph per parity, each with event nodes around every kernel
+    cudaGraphExec_t ge[2][2] = {};
+    for (int r = 0; r < reps && rc == KAMINO_OK; r++) {
+        int cu = h->cur_uv, cr = h->cur_r;
+        cudaGraphExec_t& x = ge[cu][cr];
+        if (!x) {
+            cudaGraph_t graph = nullptr;
+            KCUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+            rc = enqueue_step(h, cu, cr, ev[cu ^ cr]);
+            cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+            if (rc || e != cudaSuccess) {
+                if (graph) cudaGraphDestroy(graph);
+                if (!rc) rc = kamino_fail(KAMINO_ERR_CUDA, "capture: %s", cudaGetErrorString(e));
+                break;
+            }
+            e = cudaGraphInstantiate(&x, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) {
+                rc = kamino_fail(KAMINO_ERR_CUDA, "instantiate: %s", cudaGetErrorString(e));
+                break;
+            }
+        }
+        if (flush_l2) KCUDA(cudaMemsetAsync(h->flush, r & 0xff, h->flush_bytes, h->stream));
+        KCUDA(cudaGraphLaunch(x, h->stream));
+        KCUDA(cudaStreamSynchronize(h->stream));
+        for (int k = 0; k < kNumKernels; k++) {
+            float t = 0;
+            KCUDA(cudaEventElapsedTime(&t, ev[cu ^ cr][k], ev[cu ^ cr][k + 1]));
+            acc[k] += t;
+        }
+        h->cur_uv ^= 1;
+        h->cur_r ^= 1;
+        h->steps++;
+        h->time += h->g.dt;
+    }
+    for (auto& a : ge)
+        for (auto& x : a)
+            if (x) cudaGraphExecDestroy(x);
+    for (auto& row : ev)
+        for (auto& e : row) cudaEventDestroy(e);
+    if (rc) return rc;
+    int n = std::min(max, kNumKernels);
+    for (int k = 0; k < n; k++) ms[k] = acc[k] / reps;
+    if (count) *count = n;
+    return KAMINO_OK;
+}
+
+// ----------------------------------------------------------------- probes
+extern "C" int kamino_probe_index(kamino_handle h, int kind, const float* phi, const float* theta, int64_t n,
+                                  int32_t* out, float* alpha)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (kind < 0 || kind > 2 || n < 0 || (n && (!phi || !theta || !out || !alpha)))
+        return kamino_fail(KAMINO_ERR_INVALID, "kamino_probe_index: bad arguments");
+    if (n == 0) return KAMINO_OK;
+    float *dp = nullptr, *dt = nullptr, *da = nullptr;
+    int* di = nullptr;
+    cudaError_t e = cudaMalloc(&dp, 4 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&dt, 4 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&da, 8 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&di, 16 * n);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dp, phi, 4 * n, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dt, theta, 4 * n, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) {
+        kk::k_probe_index<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(h->g, kind, dp, dt, n, di, da);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, di, 16 * n, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(alpha, da, 8 * n, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(dp);
+    cudaFree(dt);
+    cudaFree(da);
+    cudaFree(di);
+    if (e != cudaSuccess) return kamino_fail(KAMINO_ERR_CUDA, "kamino_probe_index: %s", cudaGetErrorString(e));
+    return KAMINO_OK;
+}
+
+extern "C" int kamino_probe_wrap(kamino_handle h, float* phi, float* theta, int64_t n, int32_t* cells)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (n < 0 || (n && (!phi || !theta || !cells)))
+        return kamino_fail(KAMINO_ERR_INVALID, "kamino_probe_wrap: bad arguments");
+    if (n == 0) return KAMINO_OK;
+    float *dp = nullptr, *dt = nullptr;
+    int* dc = nullptr;
+    cudaError_t e = cudaMalloc(&dp, 4 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&dt, 4 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&dc, 8 * n);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dp, phi, 4 * n, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dt, theta, 4 * n, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) {
+        kk::k_probe_wrap<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(h->g, dp, dt, n, dc);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(phi, dp, 4 * n, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(theta, dt, 4 * n, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(cells, dc, 8 * n, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(dp);
+    cudaFree(dt);
+    cudaFree(dc);
+    if (e != cudaSuccess) return kamino_fail(KAMINO_ERR_CUDA, "kamino_probe_wrap: %s", cudaGetErrorString(e));
+    return KAMINO_OK;
+}
+
+// --------------------------------------------------------------- host memory
+extern "C" int kamino_host_alloc(size_t bytes, void** out)
+{
+    if (!out) return kamino_fail(KAMINO_ERR_INVALID, "null out");
+    KCUDA(cudaMallocHost(out, bytes ? bytes : 1));
+    return KAMINO_OK;
+}
+
+extern "C" int kamino_host_free(void* p)
+{
+    if (p) KCUDA(cudaFreeHost(p));
+    return KAMINO_OK;
+}
