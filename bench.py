@@ -1,0 +1,345 @@
+"""Benchmark of the GB300 Kamino step: cell-steps/s at nTheta=1024 x nPhi=2048.
+
+Workload (the precision-form configuration): one sphere, radius 1, nTheta=1024,
+nPhi=2048, dt=0.001, seeded stream function with l <= 32 plus one seeded
+Gaussian vortex (sigma = 0.1 rad), thickness 1 + 0.05 U(-1,1); FP32 step with
+modes |m| <= 4 solved in FP64.  A "step" is one stepForward of that sphere.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value: device time of K steps (CUDA events on the solver's stream, a 256 MiB
+  buffer written between steps so each step starts with a cold L2; the state
+  is 25 MB and would otherwise sit in the 129 MB L2).
+e2e:   the same steps through the public C ABI with host buffers: every step
+  copies u_phi, u_theta, thickness in from pinned host memory, steps, and
+  copies them back.
+--impl reference: the reference has no CPU implementation of this path, so
+  the reference arm times the CPU port of its step (oracle/, FP64, all host
+  threads) on the same configuration, plus the reference's own CUDA kernels
+  on this GPU as extra information.
+With N > 1 (torchrun), every rank advances its own sphere (replicas; the
+path does not shard) and rank 0 prints the aggregate.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NT, DT, LMAX, SEED = 1024, 0.001, 32, 1
+METRIC = "cell-steps/s at 1024x2048, batched/served vs plain; p99 latency @1e-5 rel err"
+UNIT = "cell-steps/s"
+STEP_BYTES_PER_CELL = 56    # algorithmic bytes per cell-step of the whole step (3-pass minimum)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def init_dist(ws):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic():
+    """DRAM bytes per k_advect launch from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_advect_nt1024.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, device):
+        self.p = None
+        self.device = device
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device),
+                 "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.p:
+            time.sleep(0.25)
+            self.p.terminate()
+            try:
+                out, _ = self.p.communicate(timeout=5)
+                self.lines = [l for l in out.splitlines() if l.strip()]
+            except Exception:
+                self.lines = []
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, f[2:]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def run_ours(args, ws, rank, local, dist):
+    import numpy as np
+    import kaminogpu_gb300 as kg
+
+    st = kg.make_initial_state(NT, lmax=LMAX, seed=SEED + rank, vortex=True)
+    cfg = kg.default_config(n_theta=NT, radius=1.0, dt=DT, fp64_modes=4, device=local)
+    s = kg.KaminoSolver(config=cfg)
+    s.load(st)
+    C = NT * 2 * NT
+    s.step_n(args.warmup)
+    s.synchronize()
+    # per-kernel timing (events around each launch, cold L2 each step)
+    kms = s.time_kernels(reps=max(3, min(args.steps, 10)), flush_l2=True)
+    s.load(st)
+    s.step_n(args.warmup)
+    s.synchronize()
+    barrier(dist)
+    with Clocks(local) as ck:
+        t0 = time.perf_counter()
+        ms = s.time_steps(args.steps, flush_l2=True)
+        wall = time.perf_counter() - t0
+    barrier(dist)
+    ms_max = max_over_ranks(dist, ms)
+    cells_total = sum_over_ranks(dist, C * args.steps)
+    value = cells_total / (ms_max / 1e3)
+
+    # e2e through the C ABI with pinned host buffers
+    L = kg.lib
+    nbytes = {kg.U_PHI: NT * 2 * NT * 4, kg.U_THETA: (NT - 1) * 2 * NT * 4, kg.THICKNESS: NT * 2 * NT * 4}
+    bufs = {}
+    for f, n in nbytes.items():
+        p = ctypes.c_void_p()
+        kg.check(L.kamino_host_alloc(n, ctypes.byref(p)))
+        bufs[f] = p
+    src = {kg.U_PHI: st["u_phi"], kg.U_THETA: st["u_theta"], kg.THICKNESS: st["thickness"]}
+    for f, p in bufs.items():
+        ctypes.memmove(p, src[f].ctypes.data, nbytes[f])
+    h = s._h
+    pitch = 2 * NT * 4
+    for _ in range(2):  # warm-up of the copy path
+        for f, p in bufs.items():
+            kg.check(L.kamino_set_state(h, f, p, pitch))
+        kg.check(L.kamino_step(h, DT))
+        for f, p in bufs.items():
+            kg.check(L.kamino_get_state(h, f, p, pitch))
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for f, p in bufs.items():
+            kg.check(L.kamino_set_state(h, f, p, pitch))
+        kg.check(L.kamino_step(h, DT))
+        for f, p in bufs.items():
+            kg.check(L.kamino_get_state(h, f, p, pitch))
+    e2e_s = time.perf_counter() - t0
+    barrier(dist)
+    e2e_max = max_over_ranks(dist, e2e_s)
+    e2e_value = cells_total / e2e_max
+    for p in bufs.values():
+        L.kamino_host_free(p)
+    launches = s.launches_per_step()
+    s.close()
+
+    if rank != 0:
+        return None
+    hbm, src_peak = peaks()
+    adv_ms = kms.get("k_advect")
+    dom = max(kms, key=kms.get)
+    # u_phi, u_theta, thickness read once and written once (8 bytes per point)
+    adv_bytes = 8 * (NT * 2 * NT + (NT - 1) * 2 * NT + NT * 2 * NT)
+    achieved = adv_bytes / (adv_ms / 1e3) / 1e9
+    traffic = committed_traffic()
+    step_ms = ms / args.steps
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 (FP64 for Fourier modes |m|<=4)",
+        "data": "synthetic: seeded l<=32 spherical-harmonic stream function + Gaussian vortex (sigma 0.1 rad), "
+                "max|u|=1; thickness 1+0.05U(-1,1)",
+        "config": {"workload": "plain solver, one sphere nTheta=1024 nPhi=2048, radius 1, dt=0.001 (precision form)",
+                   "sampler": "cell-exact", "fp64_modes": 4, "l2": "256 MiB buffer written before every timed step",
+                   "parallelism": "replicas" if ws > 1 else "single GPU", "wall_s_timed_region": wall},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": sum(nbytes.values()),
+                "d2h_bytes_per_step": sum(nbytes.values())},
+        "gpu_launches": launches * args.steps,
+        "roofline": {"bound": "hbm", "kernel": "k_advect", "achieved": achieved, "peak": hbm,
+                     "peak_source": src_peak, "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": adv_bytes, "avg_launch_ms": adv_ms},
+        "step_roofline": {"bytes_per_cell_step": STEP_BYTES_PER_CELL,
+                          "achieved": STEP_BYTES_PER_CELL * C / (step_ms / 1e3) / 1e9, "peak": hbm,
+                          "frac": STEP_BYTES_PER_CELL * C / (step_ms / 1e3) / 1e9 / hbm, "unit": "GB/s"},
+        "kernel_ms": kms,
+        "dominant_kernel": dom,
+        "clocks": ck.summary(),
+    }
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(st, samples=1)
+    return out
+
+
+def cpu_baseline(st, samples=1):
+    """The oracle's FP64 CPU step on a bounded sample: `samples` steps of the
+    same sphere, all host threads."""
+    from oracle import oracle as orc
+    cores = orc.set_threads(os.cpu_count() or 1)
+    o = orc.Oracle(NT, 1.0, DT)
+    o.load(st)
+    t0 = time.perf_counter()
+    o.step(samples)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": NT * 2 * NT * samples / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d FP64 step(s) of the nTheta=1024 sphere (%.1f s)" % (samples, dt)}
+
+
+def run_reference(args, ws, rank):
+    import kaminogpu_gb300 as kg
+    if rank != 0:
+        return None
+    st = kg.make_initial_state(NT, lmax=LMAX, seed=SEED, vortex=True)
+    from oracle import oracle as orc
+    cores = orc.set_threads(os.cpu_count() or 1)
+    o = orc.Oracle(NT, 1.0, DT)
+    o.load(st)
+    o.step(1)  # warm-up
+    t0 = time.perf_counter()
+    o.step(args.steps)
+    dt = time.perf_counter() - t0
+    value = NT * 2 * NT * args.steps / dt
+    out = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": 1,
+        "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic: same seeded state as the ours arm",
+        "config": {"workload": "plain solver, one sphere nTheta=1024 nPhi=2048, radius 1, dt=0.001 (precision form)",
+                   "implementation": "CPU port of the reference step (oracle/kamino_oracle.c), OpenMP"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "%d FP64 steps of the nTheta=1024 sphere" % args.steps},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    if orc.have_reference_gpu():
+        try:
+            r = orc.RefGPU(NT, 1.0, DT)
+            r.load(st)
+            r.step(2)
+            ms, stages = r.time_steps(max(args.steps, 5))
+            n = max(args.steps, 5)
+            out["reference_gpu_kernels"] = {
+                "value": NT * 2 * NT * n / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / n,
+                "stage_ms": {"advection": stages[0] / n, "geometric": stages[1] / n, "projection": stages[2] / n},
+                "what": "the reference's own CUDA kernels (compiled from its sources for sm_103a) with cuFFT, "
+                        "in stepForward order on this GPU"}
+            r.close()
+        except Exception as e:  # the CPU arm stands on its own
+            out["reference_gpu_kernels"] = {"unavailable": str(e)}
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    ws, rank, local = dist_env()
+    dist = init_dist(ws)
+    if args.impl == "reference":
+        out = run_reference(args, ws, rank)
+    else:
+        out = run_ours(args, ws, rank, local, dist)
+    if out is not None and rank == 0:
+        print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -72,7 +72,17 @@ enum kamino_flags {
      * the configured dt (KaminoSolver.cu:199, KaminoCore.cu:871). */
     KAMINO_F_HONOR_STEP_DT = 1u << 2,
     /* Skip writing the pressure field (it is an intermediate of the step). */
-    KAMINO_F_NO_PRESSURE_OUT = 1u << 3
+    KAMINO_F_NO_PRESSURE_OUT = 1u << 3,
+    /* Evaluate sample positions in radians with the reference's own
+     * float/double rounding (KaminoCore.cu:11-52), so the pole-wrap index
+     * map is bit-exact with the reference kernels.  Without this flag,
+     * positions are kept as an exact integer cell index plus an FP32
+     * fraction and the pole remap (theta -> -theta, phi -> phi + pi) is done
+     * in index arithmetic; that is the reference's algorithm with less
+     * rounding error: the radian form misplaces phi + pi by up to ~3e-5
+     * cells at nTheta = 1024 (pi/h != nTheta in float), which the RK2
+     * midpoint cancellation on the pole rows turns into O(1) differences. */
+    KAMINO_F_REFERENCE_ROUNDING = 1u << 4
 };
 
 /* Positional configKamino.txt fields (main.cu:17-45) plus extensions. */

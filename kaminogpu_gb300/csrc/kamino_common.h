@@ -32,6 +32,7 @@ struct KGeo {
     float R;      // radiusGlobal
     float dt;     // timeStepGlobal
     float cofTheta;     // dt / R (float division, KaminoCore.cu:204)
+    float cellTheta;    // dt / (R h): theta displacement in cells per unit velocity
     float pi_up;        // smallest float > M_PI: theta > M_PI  <=>  theta >= pi_up
     float wrap_phi_hi;  // smallest float x with floorf((float)(x / M_2PI)) >= 1
     int pitch;          // floats per row (== np)
@@ -49,9 +50,13 @@ struct KBufs {
     float* cv;       // geometric scratch: v at cell centres
     float* p;        // pressure
     float2* spec;    // spectrum, [mode m-1][row], m = 1..nt
+    float2* sol;     // per-mode solution, [row][mode m-1]
+    double* s64;     // FP64 solve multipliers, s64_stride(nt) doubles per FP64 mode
     // per-row tables
     float* cof_c;    // dt / (R sinf((j+1/2)h))   (centred rows, u_phi rows)
     float* cof_v;    // dt / (R sinf((j+1)h))     (u_theta rows)
+    float* cell_c;   // dt / (R sin((j+1/2)h) h): velocity -> cells, centred rows
+    float* cell_v;   // dt / (R sin((j+1)h) h):   u_theta rows
     float* gfac;     // G = dt cosf(theta) / (R sinf(theta)) at (j+1/2)h
     float* negHs;    // -h * sinf((j+1/2)h)
     float* divf;     // (1/sinf(theta_j)) / h

@@ -26,7 +26,7 @@
 namespace kdev {
 
 // validateCoord with the reference's exact arithmetic (KaminoCore.cu:11-29).
-__device__ __noinline__ float ref_validate(float& phi, float& theta)
+__device__ __forceinline__ float ref_validate(float& phi, float& theta)
 {
     float ret = 1.0f;
     {
@@ -86,8 +86,10 @@ __device__ __forceinline__ SampleIndex sample_index(float phiRaw, float thetaRaw
     s.flipped = wrap_coord(phi, theta, g);
     float nphi = __fmul_rn(phi, g.invh), nth = __fmul_rn(theta, g.invh);
     float fp = floorf(nphi), ft = floorf(nth);
-    s.ap = __fsub_rn(nphi, fp);
-    s.at = __fsub_rn(nth, ft);
+    // alpha = normed - (float)(int)floor(normed): adding +0 turns a -0.0
+    // floor into the +0.0 that the int round trip gives
+    s.ap = __fsub_rn(nphi, __fadd_rn(fp, 0.0f));
+    s.at = __fsub_rn(nth, __fadd_rn(ft, 0.0f));
     s.ip = ((int)fp) & g.mask;
     // After validateCoord theta is in [0, pi], so thetaIndex is in [0, nt].
     // The clamp only matters for non-finite input, where it keeps every read
@@ -150,10 +152,106 @@ __device__ __forceinline__ float advect_point(const float* __restrict__ u, const
     return sample<KIND>(field, pPhi, pTheta, g, vf && KIND != KIND_CENTERED);
 }
 
+// ------------------------------------------------- cell-exact positions
+// A position is a grid point (i, j) plus a small FP32 offset (fp, ft) in
+// cells, so the integer part is exact and the fraction keeps full relative
+// precision.  The staggering shifts of the samplers are exact small
+// constants, the phi seam is an integer mask, and the pole remap of
+// validateCoord (theta < 0 or theta > pi: theta -> -theta or 2pi - theta,
+// phi -> phi + pi) is exact integer/fraction arithmetic with pi = nTheta
+// cells.  Same branches and blends as the reference samplers.
+template <int KIND>
+__device__ __forceinline__ SampleIndex cell_index(int i, int j, float fp, float ft, const KGeo& g)
+{
+    SampleIndex s;
+    float kp = floorf(fp), kt = floorf(ft);
+    s.ap = fp - kp;
+    s.at = ft - kt;
+    int ip = i + (int)kp, it = j + (int)kt;
+    s.flipped = false;
+    if (it < 0) {  // theta < 0: reflect through the north pole
+        s.flipped = true;
+        ip += g.half;
+        if (s.at == 0.0f) {
+            it = -it;
+        } else {
+            it = -it - 1;
+            s.at = 1.0f - s.at;
+        }
+    } else if (it >= g.nt && (it > g.nt || s.at > 0.0f)) {  // theta > pi
+        s.flipped = true;
+        ip += g.half;
+        if (s.at == 0.0f) {
+            it = 2 * g.nt - it;
+        } else {
+            it = 2 * g.nt - it - 1;
+            s.at = 1.0f - s.at;
+        }
+    }
+    s.ip = ip & g.mask;
+    s.it = min(max(it, 0), g.nt);  // only non-finite input can need this
+    const int pole_row = (KIND == KIND_VTHETA) ? g.nt - 2 : g.nt - 1;
+    s.pole = (s.it == 0 && s.flipped) || s.it == pole_row;
+    return s;
+}
+
+__device__ __forceinline__ float lerp2(float a, float b, float t) { return __fmaf_rn(t, b - a, a); }
+
+template <int KIND>
+__device__ __forceinline__ float sample_cell(const float* __restrict__ f, int i, int j, float fp, float ft,
+                                             const KGeo& g, bool vec_flip)
+{
+    SampleIndex s = cell_index<KIND>(i, j, fp, ft, g);
+    const int i0 = s.ip, i1 = (s.ip + 1) & g.mask;
+    const float* r0 = f + s.it * g.pitch;
+    float v00 = __ldg(r0 + i0), v01 = __ldg(r0 + i1);
+    if (s.pole) {
+        const int j0 = (i0 + g.half) & g.mask, j1 = (i1 + g.half) & g.mask;
+        float v10 = __ldg(r0 + j0), v11 = __ldg(r0 + j1);
+        float lo = lerp2(v00, v01, s.ap), hi = lerp2(v10, v11, s.ap);
+        if (vec_flip) hi = -hi;
+        float w = (KIND == KIND_VPHI) ? s.at : 0.5f * s.at;
+        float r = lerp2(lo, hi, w);
+        return (vec_flip && s.flipped) ? -r : r;
+    }
+    const float* r1 = r0 + g.pitch;
+    float v10 = __ldg(r1 + i0), v11 = __ldg(r1 + i1);
+    float r = lerp2(lerp2(v00, v01, s.ap), lerp2(v10, v11, s.ap), s.at);
+    return (vec_flip && s.flipped) ? -r : r;
+}
+
+// RK2 back-trace in cells.  (cgp, cgt) is the grid point's staggering
+// offset in cells (u_phi: -1/2, 1/2; u_theta: 0, 1; centred: 0, 1/2); the
+// samplers' own offsets are u_phi (-1/2, 1/2), u_theta (0, 1), centred
+// (0, 1/2), so each sample position is (i, j) + (cg - so) - d exactly.
+// cP, cT convert velocity to displacement in cells (dt / (R sin(theta) h),
+// dt / (R h)); cP uses the grid point's latitude as the reference does.
+template <int KIND>
+__device__ __forceinline__ float advect_cell(const float* __restrict__ u, const float* __restrict__ v,
+                                             const float* __restrict__ field, int i, int j, float cP, float cT,
+                                             const KGeo& g)
+{
+    constexpr float cgp = (KIND == KIND_VPHI) ? -0.5f : 0.0f;
+    constexpr float cgt = (KIND == KIND_VTHETA) ? 1.0f : 0.5f;
+    constexpr float ou_p = cgp + 0.5f, ou_t = cgt - 0.5f;  // offsets for the u_phi sampler
+    constexpr float ov_p = cgp, ov_t = cgt - 1.0f;         // u_theta sampler
+    // a field's own sampler offset equals its staggering: offset 0
+    const bool vf = (g.flags & KAMINO_F_POLE_SIGN_FLIP) != 0;
+    float gu = sample_cell<KIND_VPHI>(u, i, j, ou_p, ou_t, g, vf);
+    float gv = sample_cell<KIND_VTHETA>(v, i, j, ov_p, ov_t, g, vf);
+    float dp = gu * cP, dtt = gv * cT;
+    float hp = 0.5f * dp, ht = 0.5f * dtt;
+    float mu = sample_cell<KIND_VPHI>(u, i, j, ou_p - hp, ou_t - ht, g, vf);
+    float mv = sample_cell<KIND_VTHETA>(v, i, j, ov_p - hp, ov_t - ht, g, vf);
+    dp = 0.5f * (mu + gu) * cP;
+    dtt = 0.5f * (mv + gv) * cT;
+    return sample_cell<KIND>(field, i, j, -dp, -dtt, g, vf && KIND != KIND_CENTERED);
+}
+
 // ------------------------------------------------------------ geometric
 // The reference's solveCubic (KaminoCore.cu:421-454) with a = 0, in FP64,
 // used only when 1 + G v <= 0 (three real roots possible).
-__device__ __noinline__ double ref_solve_cubic64(double b, double c)
+__device__ __forceinline__ double ref_solve_cubic64(double b, double c)
 {
     const double eps = (double)1e-7f;
     double q = (0.0 - 3 * b) / 9.0;

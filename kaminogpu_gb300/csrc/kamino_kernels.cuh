@@ -1,6 +1,6 @@
 // kamino_kernels.cuh — the per-step kernels of one sphere.
 //
-// One step (KaminoSolver::stepForward, KaminoSolver.cu:197-221) is five
+// One step (KaminoSolver::stepForward, KaminoSolver.cu:197-221) is six
 // launches on the handle's stream, replayed from a CUDA graph:
 //   k_advect      RK2 semi-Lagrangian u_phi, u_theta, thickness + particles
 //                 (advection(), KaminoCore.cu:344-384)
@@ -10,11 +10,12 @@
 //                 divergence (fillDivergenceKernel, :587-638) and the forward
 //                 real FFT of every latitude row; writes the spectrum
 //                 mode-major (replaces cuFFT INVERSE + shiftFKernel, :763-775)
-//   k_solve       one warp per Fourier mode: partitioned tridiagonal solve
-//                 in theta (replaces crKernel x2, tdm.cu:3-96, :779-792);
-//                 modes |m| <= fp64_modes in FP64
-//   k_ifft_grad   inverse real FFT per row and the pressure gradient
-//                 (copy2UFourier .. applyPressurePhi, :796-839)
+//   k_solve       one CTA per Fourier mode: tridiagonal solve in theta
+//                 (replaces crKernel x2, tdm.cu:3-96, :779-792); modes
+//                 |m| <= fp64_modes in FP64; writes the solution row-major
+//   k_ifft_u      inverse real FFT per row, pressure, u_phi gradient update
+//                 (copy2UFourier .. shiftUKernel, applyPressurePhi, :796-839)
+//   k_vgrad       u_theta gradient update (applyPressureTheta, :705-722)
 // Fields are dense [row][nPhi] float rows with nTheta+2 rows allocated; rows
 // past the data stay zero, which defines the reference's out-of-range reads.
 #pragma once
@@ -26,8 +27,8 @@ namespace kk {
 using namespace kdev;
 
 constexpr int ADV_THREADS = 256;
-constexpr int FFT_ROWS = 4;      // latitude rows per CTA in k_div_fft / k_ifft_grad
-constexpr int SOLVE_WARPS = 4;   // modes per CTA in k_solve
+constexpr int ELEM_THREADS = 256;
+constexpr int SOLVE_THREADS = 128;  // threads per Fourier mode in k_solve (nTheta >= 128)
 
 // ----------------------------------------------------------- per-row tables
 // Evaluated on the device with the reference's own float expressions
@@ -50,6 +51,8 @@ __global__ void k_tables(KGeo g, KBufs b)
 }
 
 // --------------------------------------------------------------- advection
+// Particles keep the reference's radian form in both sampler modes: their
+// state is (phi, theta) in radians and validateCoord is applied to it.
 __device__ __forceinline__ void advect_particle(const KGeo& g, const float* __restrict__ u,
                                                 const float* __restrict__ v, float2 pos, float2& out)
 {
@@ -83,7 +86,9 @@ __device__ __forceinline__ void advect_particle(const KGeo& g, const float* __re
 }
 
 // Blocks [0, nb_u) advect u_phi, then u_theta, then thickness, then
-// particles; each thread one grid point or one particle.
+// particles; each thread one grid point or one particle.  REF selects the
+// reference-rounding (radian) sampler, otherwise the cell-exact one.
+template <bool REF>
 __global__ void __launch_bounds__(ADV_THREADS) k_advect(KGeo g, KBufs b, int suv, int duv, int sr, int dr,
                                                          int nb_u, int nb_v, int nb_r)
 {
@@ -91,33 +96,37 @@ __global__ void __launch_bounds__(ADV_THREADS) k_advect(KGeo g, KBufs b, int suv
     const float* __restrict__ v = b.v[suv];
     int blk = blockIdx.x;
     const int lg = g.log2nt + 1;  // log2(nPhi)
-    if (blk < nb_u) {
-        int idx = blk * ADV_THREADS + threadIdx.x;
-        if (idx >= g.nt * g.np) return;
+    if (blk < nb_u + nb_v + nb_r) {
+        const int which = blk < nb_u ? 0 : (blk < nb_u + nb_v ? 1 : 2);
+        const int b0 = which == 0 ? 0 : (which == 1 ? nb_u : nb_u + nb_v);
+        int idx = (blk - b0) * ADV_THREADS + threadIdx.x;
+        if (idx >= (which == 1 ? g.nt - 1 : g.nt) * g.np) return;
         int j = idx >> lg, i = idx & g.mask;
-        float gPhi = __fmul_rn((float)i - 0.5f, g.h), gTheta = __fmul_rn((float)j + 0.5f, g.h);
-        b.u[duv][idx] = advect_point<KIND_VPHI>(u, v, u, gPhi, gTheta, __ldg(b.cof_c + j), g);
+        float val;
+        if (REF) {
+            if (which == 0) {
+                float gPhi = __fmul_rn((float)i - 0.5f, g.h), gTheta = __fmul_rn((float)j + 0.5f, g.h);
+                val = advect_point<KIND_VPHI>(u, v, u, gPhi, gTheta, __ldg(b.cof_c + j), g);
+            } else if (which == 1) {
+                float gPhi = __fmul_rn((float)i, g.h), gTheta = __fmul_rn((float)j + 1.0f, g.h);
+                val = advect_point<KIND_VTHETA>(u, v, v, gPhi, gTheta, __ldg(b.cof_v + j), g);
+            } else {
+                float gPhi = __fmul_rn((float)i, g.h), gTheta = __fmul_rn((float)j + 0.5f, g.h);
+                val = advect_point<KIND_CENTERED>(u, v, b.rho[sr], gPhi, gTheta, __ldg(b.cof_c + j), g);
+            }
+        } else {
+            if (which == 0)
+                val = advect_cell<KIND_VPHI>(u, v, u, i, j, __ldg(b.cell_c + j), g.cellTheta, g);
+            else if (which == 1)
+                val = advect_cell<KIND_VTHETA>(u, v, v, i, j, __ldg(b.cell_v + j), g.cellTheta, g);
+            else
+                val = advect_cell<KIND_CENTERED>(u, v, b.rho[sr], i, j, __ldg(b.cell_c + j), g.cellTheta, g);
+        }
+        float* dst = which == 0 ? b.u[duv] : (which == 1 ? b.v[duv] : b.rho[dr]);
+        dst[idx] = val;
         return;
     }
-    blk -= nb_u;
-    if (blk < nb_v) {
-        int idx = blk * ADV_THREADS + threadIdx.x;
-        if (idx >= (g.nt - 1) * g.np) return;
-        int j = idx >> lg, i = idx & g.mask;
-        float gPhi = __fmul_rn((float)i, g.h), gTheta = __fmul_rn((float)j + 1.0f, g.h);
-        b.v[duv][idx] = advect_point<KIND_VTHETA>(u, v, v, gPhi, gTheta, __ldg(b.cof_v + j), g);
-        return;
-    }
-    blk -= nb_v;
-    if (blk < nb_r) {
-        int idx = blk * ADV_THREADS + threadIdx.x;
-        if (idx >= g.nt * g.np) return;
-        int j = idx >> lg, i = idx & g.mask;
-        float gPhi = __fmul_rn((float)i, g.h), gTheta = __fmul_rn((float)j + 0.5f, g.h);
-        b.rho[dr][idx] = advect_point<KIND_CENTERED>(u, v, b.rho[sr], gPhi, gTheta, __ldg(b.cof_c + j), g);
-        return;
-    }
-    blk -= nb_r;
+    blk -= nb_u + nb_v + nb_r;
     int64_t k = (int64_t)blk * ADV_THREADS + threadIdx.x;
     if (k >= b.npart) return;
     float2 out;
@@ -126,7 +135,7 @@ __global__ void __launch_bounds__(ADV_THREADS) k_advect(KGeo g, KBufs b, int suv
 }
 
 // --------------------------------------------------------------- geometric
-__global__ void __launch_bounds__(256) k_geo_centers(KGeo g, KBufs b, int src)
+__global__ void __launch_bounds__(ELEM_THREADS) k_geo_centers(KGeo g, KBufs b, int src)
 {
     int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= g.nt * g.np) return;
@@ -137,7 +146,7 @@ __global__ void __launch_bounds__(256) k_geo_centers(KGeo g, KBufs b, int src)
     float uPrev = 0.5f * __fadd_rn(__ldg(u + idx), __ldg(u + (idx & ~g.mask) + ((i + 1) & g.mask)));
     float vPrev;
     if (j == 0 || j == g.nt - 1) {
-        const float* vr = v + (size_t)(j == 0 ? 0 : g.nt - 2) * g.np;
+        const float* vr = v + (j == 0 ? 0 : g.nt - 2) * g.np;
         vPrev = __fmaf_rn(0.75f, __ldg(vr + i), 0.25f * __ldg(vr + ((i + g.half) & g.mask)));
     } else {
         vPrev = 0.5f * __fadd_rn(__ldg(v + idx - g.np), __ldg(v + idx));
@@ -149,18 +158,104 @@ __global__ void __launch_bounds__(256) k_geo_centers(KGeo g, KBufs b, int src)
     b.cv[idx] = vNext;
 }
 
-// ------------------------------------------------------- divergence + FFT
-// MODE 0: from centres: write u**, v** and the spectrum (fused step)
-// MODE 1: from centres: write u**, v** only (geometric stage alone)
-// MODE 2: from faces: spectrum of the divergence of (u, v) (projection alone)
+// assignPhiKernel / assignThetaKernel (KaminoCore.cu:517-549) alone, for the
+// geometric stage called by itself; the fused step does this in k_div_fft.
+__global__ void __launch_bounds__(ELEM_THREADS) k_assign(KGeo g, KBufs b, int uv_out)
+{
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= g.nt * g.np) return;
+    const int lg = g.log2nt + 1;
+    int j = idx >> lg, i = idx & g.mask;
+    const size_t row = (size_t)j * g.np;
+    b.u[uv_out][idx] = 0.5f * __fadd_rn(__ldg(b.cu + row + ((i - 1) & g.mask)), __ldg(b.cu + idx));
+    if (j < g.nt - 1) b.v[uv_out][idx] = 0.5f * __fadd_rn(__ldg(b.cv + idx), __ldg(b.cv + idx + g.np));
+}
+
+// ------------------------------------------------------------ FFT (Stockham)
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+
+// 4-point DFT in place, kernel e^{-2 pi i/4} = -i (forward) or +i (inverse)
+template <bool INV>
+__device__ __forceinline__ void dft4(float2& a, float2& b, float2& c, float2& d)
+{
+    float2 apc = f2add(a, c), amc = f2sub(a, c), bpd = f2add(b, d), bmd = f2sub(b, d);
+    float2 sb = INV ? make_float2(-bmd.y, bmd.x) : make_float2(bmd.y, -bmd.x);
+    a = f2add(apc, bpd);
+    c = f2sub(apc, bpd);
+    b = f2add(amc, sb);
+    d = f2sub(amc, sb);
+}
+
+// Complex FFT of length N (power of two, >= 16) by T = N/4 threads, Stockham
+// autosort: radix-4 stages, then one radix-2 stage when log2 N is odd.
+// Thread t enters holding x[t + r T], r = 0..3, and the transform ends in
+// natural order in the returned shared buffer.  tw[k] = e^{-2 pi i k/N}.
+template <bool INV>
+__device__ __forceinline__ float2* stockham(float2 v[4], float2* bufA, float2* bufB, int N, int t,
+                                            const float2* __restrict__ tw)
+{
+    const int T = N >> 2;
+    float2* out = bufA;
+    int Ns = 1, ls = 0;
+    while (true) {
+        if (4 * Ns <= N) {
+            const int k = t & (Ns - 1);
+            if (Ns > 1) {
+                const int step = N >> (ls + 2);
+#pragma unroll
+                for (int r = 1; r < 4; r++) {
+                    float2 w = __ldg(tw + r * k * step);
+                    if (INV) w.y = -w.y;
+                    v[r] = cmul(w, v[r]);
+                }
+            }
+            dft4<INV>(v[0], v[1], v[2], v[3]);
+            const int base = ((t - k) << 2) + k;
+#pragma unroll
+            for (int r = 0; r < 4; r++) out[base + r * Ns] = v[r];
+            Ns <<= 2;
+            ls += 2;
+        } else {  // radix-2, Ns = N/2: butterflies t and t + T
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const int idx = t + q * T;
+                float2 w = __ldg(tw + idx);
+                if (INV) w.y = -w.y;
+                float2 y = cmul(w, v[q + 2]);
+                out[idx] = f2add(v[q], y);
+                out[idx + Ns] = f2sub(v[q], y);
+            }
+            Ns <<= 1;
+            ls += 1;
+        }
+        __syncthreads();
+        if (Ns >= N) return out;
+#pragma unroll
+        for (int r = 0; r < 4; r++) v[r] = out[t + r * T];
+        out = (out == bufA) ? bufB : bufA;
+    }
+}
+
+// Rows per CTA for the per-row FFT kernels: N/4 threads per row, up to 256
+// threads per CTA.
+__host__ __device__ inline int fft_rows_per_cta(int nt) { return nt >= 1024 ? 1 : 1024 / nt; }
+
+// Divergence and forward real FFT of latitude rows.
+// MODE 0: from cell centres, also writing u**, v** (the fused step)
+// MODE 2: from face velocities (projection stage called by itself)
+// Writes c_m = (1/nPhi) sum_j div_j e^{-i m phi_j}, m = 1..nt, mode-major:
+// spec[(m-1)*nt + row].  c_0 (the dropped m = 0 mode) is never formed.
 template <int MODE>
-__global__ void __launch_bounds__(32 * FFT_ROWS) k_div_fft(KGeo g, KBufs b, int uv_in, int uv_out)
+__global__ void __launch_bounds__(512) k_div_fft(KGeo g, KBufs b, int uv_in, int uv_out)
 {
     extern __shared__ float2 sm2[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int r0 = blockIdx.x * FFT_ROWS, j = r0 + warp;
-    const int nt = g.nt, np = g.np, mask = g.mask;
-    float2* buf = sm2 + warp * (nt + 1);
+    const int N = g.nt, T = N >> 2, rpc = fft_rows_per_cta(N);
+    const int lr = threadIdx.x / T, t = threadIdx.x - lr * T;
+    const int j = blockIdx.x * rpc + lr;
+    const int np = g.np, mask = g.mask;
+    float2* bufA = sm2 + (size_t)lr * 2 * N;
+    float2* bufB = bufA + N;
     const float* __restrict__ cu = b.cu;
     const float* __restrict__ cv = b.cv;
     const float* __restrict__ uf = b.u[uv_in];
@@ -169,333 +264,399 @@ __global__ void __launch_bounds__(32 * FFT_ROWS) k_div_fft(KGeo g, KBufs b, int 
     float* __restrict__ vo = b.v[uv_out];
     const float fct = __ldg(b.divf + j), sN = __ldg(b.sinN + j), sS = __ldg(b.sinS + j);
     const size_t row = (size_t)j * np;
-    for (int k = lane; k < nt; k += 32) {
+    float2 v[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const int k = t + r * T;
         float d[2];
 #pragma unroll
         for (int e = 0; e < 2; e++) {
             const int i = 2 * k + e;
             float uW, uE, vN, vS;
-            if (MODE != 2) {
+            if (MODE == 0) {
                 float cm1 = __ldg(cu + row + ((i - 1) & mask)), c0 = __ldg(cu + row + i);
                 float c1 = __ldg(cu + row + ((i + 1) & mask));
                 uW = 0.5f * __fadd_rn(cm1, c0);  // assignPhiKernel, KaminoCore.cu:531-533
                 uE = 0.5f * __fadd_rn(c0, c1);
                 float cvj = __ldg(cv + row + i);
                 vN = j > 0 ? 0.5f * __fadd_rn(__ldg(cv + row - np + i), cvj) : 0.0f;  // :546-548
-                vS = j < nt - 1 ? 0.5f * __fadd_rn(cvj, __ldg(cv + row + np + i)) : 0.0f;
+                vS = j < N - 1 ? 0.5f * __fadd_rn(cvj, __ldg(cv + row + np + i)) : 0.0f;
                 uo[row + i] = uW;
-                if (j < nt - 1) vo[row + i] = vS;
+                if (j < N - 1) vo[row + i] = vS;
             } else {
                 uW = __ldg(uf + row + i);
                 uE = __ldg(uf + row + ((i + 1) & mask));
                 vN = j > 0 ? __ldg(vf + row - np + i) : 0.0f;
-                vS = j < nt - 1 ? __ldg(vf + row + i) : 0.0f;
+                vS = j < N - 1 ? __ldg(vf + row + i) : 0.0f;
             }
             // fillDivergenceKernel, KaminoCore.cu:625-632
             float termTheta = __fmul_rn(fct, __fsub_rn(__fmul_rn(vS, sS), __fmul_rn(vN, sN)));
             float termPhi = __fmul_rn(fct, __fsub_rn(uE, uW));
             d[e] = __fadd_rn(termTheta, termPhi);
         }
-        if (MODE != 1) buf[bitrev(k, g.log2nt)] = make_float2(d[0], d[1]);
+        v[r] = make_float2(d[0], d[1]);  // z_k = f_{2k} + i f_{2k+1}
     }
-    if (MODE == 1) return;
-    __syncwarp();
-    fft_dit_warp<false>(buf, nt, g.log2nt, b.tw, lane);
-    // Real-FFT unpacking: c_m = (1/nPhi) [E_m + e^{-i pi m/nt} O_m] with
-    // E, O from Z_m and conj(Z_{nt-m}).  Pairs (m, nt-m) are updated in place
-    // by one lane; c_nt (real) goes to slot 0 whose c_0 is never used.
+    const float2* Z = stockham<false>(v, bufA, bufB, N, t, b.tw);
+    // c_m = (1/nPhi)[E_m + e^{-i pi m/N} O_m], E/O from Z_m and conj(Z_{N-m});
+    // pairs (m, N-m) share their inputs.
     const float scale = 1.0f / (float)np;
-    for (int m = lane; m <= nt / 2; m += 32) {
-        if (m == 0) {
-            float2 z0 = buf[0];
-            buf[0] = make_float2((z0.x - z0.y) * scale, 0.0f);
+    for (int m = t; m <= N / 2; m += T) {
+        if (m == 0) {  // c_N (real): Re Z_0 - Im Z_0
+            float2 z0 = Z[0];
+            b.spec[(size_t)(N - 1) * N + j] = make_float2((z0.x - z0.y) * scale, 0.0f);
             continue;
         }
-        const int mb = nt - m;
-        float2 za = buf[m], zb = buf[mb];
+        const int mb = N - m;
+        float2 za = Z[m], zb = Z[mb];
         float2 wa = __ldg(b.rt + m), wb = __ldg(b.rt + mb);
         float er = 0.5f * (za.x + zb.x), ei = 0.5f * (za.y - zb.y);
         float orr = 0.5f * (za.y + zb.y), oi = -0.5f * (za.x - zb.x);
-        buf[m] = make_float2((er + wa.x * orr - wa.y * oi) * scale, (ei + wa.x * oi + wa.y * orr) * scale);
-        if (mb != m) {
-            // (Zb, Za) pair: E' = conj(E), O' = conj(O)
-            float er2 = er, ei2 = -ei, or2 = orr, oi2 = -oi;
-            buf[mb] = make_float2((er2 + wb.x * or2 - wb.y * oi2) * scale,
-                                  (ei2 + wb.x * oi2 + wb.y * or2) * scale);
-        }
-    }
-    __syncthreads();
-    // mode-major store: spec[(m-1)*nt + row], FFT_ROWS rows per 32-byte run
-    for (int t = threadIdx.x; t < nt * FFT_ROWS; t += blockDim.x) {
-        int mi = t / FFT_ROWS, r = t - mi * FFT_ROWS;
-        b.spec[(size_t)mi * nt + r0 + r] = sm2[r * (nt + 1) + ((mi + 1) & (nt - 1))];
+        b.spec[(size_t)(m - 1) * N + j] =
+            make_float2((er + wa.x * orr - wa.y * oi) * scale, (ei + wa.x * oi + wa.y * orr) * scale);
+        if (mb != m)  // (Zb, Za): E' = conj(E), O' = conj(O)
+            b.spec[(size_t)(mb - 1) * N + j] =
+                make_float2((er + wb.x * orr + wb.y * oi) * scale, (-ei - wb.x * oi + wb.y * orr) * scale);
     }
 }
 
 // ------------------------------------------------------------- mode solve
-// Normalised rows a_i x_{i-1} + x_i + c_i x_{i+1} = d_i (complex d).  A lane
-// owns P = nt/32 consecutive rows.  Eliminating inside the block leaves each
-// interior row coupled only to the block's first and last unknowns, and
-// those first/last rows form a tridiagonal system of 64 unknowns (two per
-// lane) solved by parallel cyclic reduction over warp shuffles.
+// Each Fourier mode m >= 1 of the pressure solves the reference's tridiagonal
+// system (precomputeABCKernel, KaminoSolver.cu:128-159; crKernel, tdm.cu)
+//   A_i x_{i-1} + B_i x_i + C_i x_{i+1} = c_i,  B_i = -(A_i + C_i + m^2/sin^2).
+// Written as the M-matrix  -A x_{i-1} + P x_i - C x_{i+1} = -c  with
+// P = A + C + s and the row dominance s = m^2/sin^2(theta_i) held
+// explicitly, elimination and cyclic reduction only ever add non-negative
+// terms (the new dominance is s_i + (A_i/P_{i-1}) s_{i-1}; the diagonal is
+// recomputed as s + |couplings|).  Nothing cancels, so FP32 keeps high
+// relative accuracy for every mode; the direct FP32 forms lose about
+// cond(T) ~ nTheta^2/m^2 ulps on the low modes.
+//
+// FP32 modes: SOLVE_THREADS threads per mode, P = nTheta/SOLVE_THREADS rows
+// per thread in registers.  Each thread eliminates inside its block so the
+// interior rows couple only to the block's first and last unknowns; those
+// 2*SOLVE_THREADS rows form a tridiagonal M-matrix solved by parallel cyclic
+// reduction in shared memory.  FP64 modes: one warp, multipliers
+// precomputed in FP64 on the host (the matrix is fixed), so the device only
+// runs the right-hand-side recurrences.
 template <typename T>
 struct Row {
-    T a, c, dr, di;
+    T a, c, s, dr, di;  // couplings (>= 0), dominance (>= 0), right-hand side
 };
 
-template <typename T>
-__device__ __forceinline__ Row<T> shfl_row_up(const Row<T>& r, int s, int lane)
+__device__ __forceinline__ float rcpf(float x) { return __frcp_rn(x); }
+
+// One cyclic-reduction step of row x with its neighbours lo (-s) and hi (+s).
+__device__ __forceinline__ Row<float> pcr_combine(const Row<float>& x, const Row<float>& lo, const Row<float>& hi)
 {
-    Row<T> o;
-    o.a = __shfl_up_sync(0xffffffffu, r.a, s);
-    o.c = __shfl_up_sync(0xffffffffu, r.c, s);
-    o.dr = __shfl_up_sync(0xffffffffu, r.dr, s);
-    o.di = __shfl_up_sync(0xffffffffu, r.di, s);
-    if (lane < s) o.a = o.c = o.dr = o.di = T(0);
+    float rl = x.a * rcpf(lo.s + lo.a + lo.c);
+    float rh = x.c * rcpf(hi.s + hi.a + hi.c);
+    Row<float> o;
+    o.a = rl * lo.a;
+    o.c = rh * hi.c;
+    o.s = x.s + rl * lo.s + rh * hi.s;
+    o.dr = x.dr + rl * lo.dr + rh * hi.dr;
+    o.di = x.di + rl * lo.di + rh * hi.di;
     return o;
 }
 
-template <typename T>
-__device__ __forceinline__ Row<T> shfl_row_down(const Row<T>& r, int s, int lane)
+// Shared-memory PCR over R rows (R a power of two); thread t owns rows
+// t*q .. t*q+q-1, q = R / nthreads (1 or 2).
+template <int Q>
+__device__ __forceinline__ void pcr_smem(Row<float> (&r)[Q], Row<float>* rs, int R, int t)
 {
-    Row<T> o;
-    o.a = __shfl_down_sync(0xffffffffu, r.a, s);
-    o.c = __shfl_down_sync(0xffffffffu, r.c, s);
-    o.dr = __shfl_down_sync(0xffffffffu, r.dr, s);
-    o.di = __shfl_down_sync(0xffffffffu, r.di, s);
-    if (lane + s >= 32) o.a = o.c = o.dr = o.di = T(0);
-    return o;
-}
-
-// One PCR reduction of row x with its neighbours at -s (lo) and +s (hi).
-template <typename T>
-__device__ __forceinline__ Row<T> pcr_combine(const Row<T>& x, const Row<T>& lo, const Row<T>& hi)
-{
-    T diag = T(1) - x.a * lo.c - x.c * hi.a;
-    T inv = T(1) / diag;
-    Row<T> o;
-    o.a = -x.a * lo.a * inv;
-    o.c = -x.c * hi.c * inv;
-    o.dr = (x.dr - x.a * lo.dr - x.c * hi.dr) * inv;
-    o.di = (x.di - x.a * lo.di - x.c * hi.di) * inv;
-    return o;
-}
-
-template <typename T>
-__device__ void solve_mode(const KGeo& g, const KBufs& b, int m, T* sa, T* sc, T* sdr, T* sdi, int lane)
-{
-    const int n = g.nt;
-    const int P = n > 32 ? n >> 5 : 1;  // rows per lane; n <= 32: one row per lane
-    auto pidx = [P](int r) { return r + r / P; };
-    float2* col = b.spec + (size_t)(m - 1) * n;
-    const T m2 = (T)m * (T)m;
-    for (int r = lane; r < n; r += 32) {
-        T A, C, B;
-        if (sizeof(T) == 8) {
-            A = (T)b.lapA64[r];
-            C = (T)b.lapC64[r];
-            B = (T)b.lapB064[r] - m2 * (T)b.lapS64[r];
-        } else {
-            A = (T)b.lapA[r];
-            C = (T)b.lapC[r];
-            B = (T)b.lapB0[r] - m2 * (T)b.lapS[r];
-        }
-        T inv = T(1) / B;
-        float2 d = col[r];
-        int q = pidx(r);
-        sa[q] = A * inv;
-        sc[q] = C * inv;
-        sdr[q] = (T)d.x * inv;
-        sdi[q] = (T)d.y * inv;
-    }
-    __syncwarp();
-    Row<T> F, L;
-    const int f = lane * P, l = f + P - 1;
-    if (n <= 32) {
-        // PCR over 32 rows, one per lane; lanes past n carry identity rows
-        // (a = c = 0) that the last real row (c = 0) never couples to.
-        int q = pidx(lane);
-        const bool real = lane < n;
-        F.a = real ? sa[q] : T(0);
-        F.c = real ? sc[q] : T(0);
-        F.dr = real ? sdr[q] : T(0);
-        F.di = real ? sdi[q] : T(0);
-        for (int s = 1; s < 32; s <<= 1) {
-            Row<T> lo = shfl_row_up(F, s, lane), hi = shfl_row_down(F, s, lane);
-            F = pcr_combine(F, lo, hi);
-        }
-        __syncwarp();
-        if (real) {
-            sdr[q] = F.dr;
-            sdi[q] = F.di;
-        }
-    } else {
-        // downward: rows f+2..l now couple x_f instead of x_{i-1}
-        for (int i = f + 2; i <= l; i++) {
-            int q = pidx(i), qm = pidx(i - 1);
-            T ai = sa[q], ci = sc[q];
-            T r = T(1) / (T(1) - ai * sc[qm]);
-            sa[q] = -ai * sa[qm] * r;
-            sc[q] = ci * r;
-            sdr[q] = (sdr[q] - ai * sdr[qm]) * r;
-            sdi[q] = (sdi[q] - ai * sdi[qm]) * r;
-        }
-        {
-            int q = pidx(l);
-            L.a = sa[q];
-            L.c = sc[q];
-            L.dr = sdr[q];
-            L.di = sdi[q];
-        }
-        // upward: rows l-2..f+1 couple x_f and x_l
-        for (int i = l - 2; i >= f + 1; i--) {
-            int q = pidx(i), qp = pidx(i + 1);
-            T ci = sc[q];
-            sa[q] = sa[q] - ci * sa[qp];
-            sc[q] = -ci * sc[qp];
-            sdr[q] = sdr[q] - ci * sdr[qp];
-            sdi[q] = sdi[q] - ci * sdi[qp];
-        }
-        {
-            int q = pidx(f);
-            T af = sa[q], cf = sc[q], dfr = sdr[q], dfi = sdi[q];
-            if (P >= 3) {
-                int q1 = pidx(f + 1);
-                T inv = T(1) / (T(1) - cf * sa[q1]);
-                F.a = af * inv;
-                F.c = -cf * sc[q1] * inv;
-                F.dr = (dfr - cf * sdr[q1]) * inv;
-                F.di = (dfi - cf * sdi[q1]) * inv;
+    for (int s = 1; s < R; s <<= 1) {
+#pragma unroll
+        for (int e = 0; e < Q; e++) rs[t * Q + e] = r[e];
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < Q; e++) {
+            const int i = t * Q + e;
+            Row<float> lo, hi;
+            if (i - s >= 0) {
+                lo = rs[i - s];
             } else {
-                F.a = af;
-                F.c = cf;
-                F.dr = dfr;
-                F.di = dfi;
+                lo.a = lo.c = lo.dr = lo.di = 0.0f;
+                lo.s = 1.0f;
             }
+            if (i + s < R) {
+                hi = rs[i + s];
+            } else {
+                hi.a = hi.c = hi.dr = hi.di = 0.0f;
+                hi.s = 1.0f;
+            }
+            r[e] = pcr_combine(r[e], lo, hi);
         }
-        // PCR over the 64 boundary rows: row 2k = F, row 2k+1 = L of lane k
-        {
-            Row<T> Bm = shfl_row_up(L, 1, lane);    // row 2k-1
-            Row<T> Ap = shfl_row_down(F, 1, lane);  // row 2k+2
-            Row<T> nF = pcr_combine(F, Bm, L);
-            Row<T> nL = pcr_combine(L, F, Ap);
-            F = nF;
-            L = nL;
-        }
-        for (int t = 1; t < 32; t <<= 1) {
-            Row<T> Fm = shfl_row_up(F, t, lane), Fp = shfl_row_down(F, t, lane);
-            Row<T> Lm = shfl_row_up(L, t, lane), Lp = shfl_row_down(L, t, lane);
-            F = pcr_combine(F, Fm, Fp);
-            L = pcr_combine(L, Lm, Lp);
-        }
-        const T xfr = F.dr, xfi = F.di, xlr = L.dr, xli = L.di;
-        for (int i = f + 1; i <= l - 1; i++) {
-            int q = pidx(i);
-            T ai = sa[q], ci = sc[q];
-            sdr[q] = sdr[q] - ai * xfr - ci * xlr;
-            sdi[q] = sdi[q] - ai * xfi - ci * xli;
-        }
-        sdr[pidx(f)] = xfr;
-        sdi[pidx(f)] = xfi;
-        sdr[pidx(l)] = xlr;
-        sdi[pidx(l)] = xli;
-    }
-    __syncwarp();
-    for (int r = lane; r < n; r += 32) {
-        int q = pidx(r);
-        col[r] = make_float2((float)sdr[q], (float)sdi[q]);
+        __syncthreads();
     }
 }
 
-// Blocks [0, nfp64) solve modes 1..nfp64 in FP64 (warp 0 only); the rest
-// solve SOLVE_WARPS FP32 modes each.
-__global__ void __launch_bounds__(32 * SOLVE_WARPS) k_solve(KGeo g, KBufs b, int nfp64)
+// FP32 solve of mode m by the whole CTA (blockDim.x = nt / P threads).
+template <int P>
+__device__ void solve_mode32(const KGeo& g, const KBufs& b, int m, Row<float>* rs)
 {
-    extern __shared__ unsigned char smraw[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int n = g.nt, stride = n + 32;
-    if ((int)blockIdx.x < nfp64) {
-        if (warp != 0) return;
-        double* base = reinterpret_cast<double*>(smraw);
-        solve_mode<double>(g, b, blockIdx.x + 1, base, base + stride, base + 2 * stride, base + 3 * stride,
-                           lane);
+    const int n = g.nt, t = threadIdx.x;
+    const float m2 = (float)m * (float)m;
+    const float2* __restrict__ col = b.spec + (size_t)(m - 1) * n;
+    float2* __restrict__ sol = b.sol + (m - 1);  // sol[row * n + m - 1]
+    if (P == 1) {
+        Row<float> r[1];
+        r[0].a = __ldg(b.lapA + t);
+        r[0].c = __ldg(b.lapC + t);
+        r[0].s = m2 * __ldg(b.lapS + t);
+        float2 d = col[t];
+        r[0].dr = -d.x;
+        r[0].di = -d.y;
+        pcr_smem<1>(r, rs, n, t);
+        float inv = rcpf(r[0].s + r[0].a + r[0].c);
+        sol[(size_t)t * n] = make_float2(r[0].dr * inv, r[0].di * inv);
         return;
     }
-    const int m = nfp64 + 1 + (blockIdx.x - nfp64) * SOLVE_WARPS + warp;
-    if (m > n) return;
-    float* base = reinterpret_cast<float*>(smraw) + (size_t)warp * 4 * stride;
-    solve_mode<float>(g, b, m, base, base + stride, base + 2 * stride, base + 3 * stride, lane);
+    const int f = t * P;
+    float A[P], C[P], S[P], Dr[P], Di[P];
+#pragma unroll
+    for (int q = 0; q < P; q++) {
+        A[q] = __ldg(b.lapA + f + q);
+        C[q] = __ldg(b.lapC + f + q);
+        S[q] = m2 * __ldg(b.lapS + f + q);
+        float2 d = col[f + q];
+        Dr[q] = -d.x;
+        Di[q] = -d.y;
+    }
+    // downward: rows q >= 2 couple x_f instead of x_{q-1}
+#pragma unroll
+    for (int q = 2; q < P; q++) {
+        float r = A[q] * rcpf(S[q - 1] + A[q - 1] + C[q - 1]);
+        A[q] = r * A[q - 1];
+        S[q] += r * S[q - 1];
+        Dr[q] += r * Dr[q - 1];
+        Di[q] += r * Di[q - 1];
+    }
+    Row<float> rr[2];
+    rr[1].a = A[P - 1];
+    rr[1].c = C[P - 1];
+    rr[1].s = S[P - 1];
+    rr[1].dr = Dr[P - 1];
+    rr[1].di = Di[P - 1];
+    // upward: rows P-3 .. 1 couple x_f and x_l
+#pragma unroll
+    for (int q = P - 3; q >= 1; q--) {
+        float r = C[q] * rcpf(S[q + 1] + A[q + 1] + C[q + 1]);
+        A[q] += r * A[q + 1];
+        C[q] = r * C[q + 1];
+        S[q] += r * S[q + 1];
+        Dr[q] += r * Dr[q + 1];
+        Di[q] += r * Di[q + 1];
+    }
+    rr[0].a = A[0];
+    rr[0].c = C[0];
+    rr[0].s = S[0];
+    rr[0].dr = Dr[0];
+    rr[0].di = Di[0];
+    if (P >= 3) {
+        float r = C[0] * rcpf(S[1] + A[1] + C[1]);
+        rr[0].c = r * C[1];
+        rr[0].s += r * S[1];
+        rr[0].dr += r * Dr[1];
+        rr[0].di += r * Di[1];
+    }
+    pcr_smem<2>(rr, rs, 2 * blockDim.x, t);
+    float iF = rcpf(rr[0].s + rr[0].a + rr[0].c), iL = rcpf(rr[1].s + rr[1].a + rr[1].c);
+    const float xfr = rr[0].dr * iF, xfi = rr[0].di * iF, xlr = rr[1].dr * iL, xli = rr[1].di * iL;
+    sol[(size_t)f * n] = make_float2(xfr, xfi);
+    sol[(size_t)(f + P - 1) * n] = make_float2(xlr, xli);
+#pragma unroll
+    for (int q = 1; q < P - 1; q++) {
+        float inv = rcpf(S[q] + A[q] + C[q]);
+        sol[(size_t)(f + q) * n] =
+            make_float2((Dr[q] + A[q] * xfr + C[q] * xlr) * inv, (Di[q] + A[q] * xfi + C[q] * xli) * inv);
+    }
 }
 
-// ---------------------------------------------------- inverse FFT + gradient
-// Rows r0..r0+FFT_ROWS-1 are updated; row r0+FFT_ROWS (when it exists) is
-// synthesised too because v at row j needs p at rows j and j+1.
-__global__ void __launch_bounds__(32 * (FFT_ROWS + 1)) k_ifft_grad(KGeo g, KBufs b, int uv_in, int uv_out,
-                                                                    int write_p)
+// Layout of the FP64 multiplier tables of one mode (host-built by
+// fp64_tables() in kamino_solver.cu): per row dn, up, bA, bC, bInv, then
+// rF[32], pl[6][64], ph[6][64], pinv[64].
+__host__ __device__ inline size_t s64_stride(int nt) { return 5 * (size_t)nt + 32 + 2 * 6 * 64 + 64; }
+
+// FP64 solve of mode m by one warp: lane k owns rows [k P, k P + P), P =
+// nt/32 (one row per lane when nt == 32).  Only the right-hand side is
+// carried; every multiplier comes from the tables.
+__device__ void solve_mode64(const KGeo& g, const KBufs& b, int m, double* sdr, double* sdi)
+{
+    const int n = g.nt, lane = threadIdx.x & 31;
+    const int P = n >> 5;
+    const double* tb = b.s64 + (size_t)(m - 1) * s64_stride(n);
+    const double *dn = tb, *up = tb + n, *bA = tb + 2 * n, *bC = tb + 3 * n, *bInv = tb + 4 * n;
+    const double *rF = tb + 5 * n, *pl = rF + 32, *ph = pl + 6 * 64, *pinv = ph + 6 * 64;
+    const float2* __restrict__ col = b.spec + (size_t)(m - 1) * n;
+    float2* __restrict__ sol = b.sol + (m - 1);
+    auto pidx = [P](int r) { return r + r / P; };
+    for (int r = lane; r < n; r += 32) {
+        float2 d = col[r];
+        sdr[pidx(r)] = -(double)d.x;
+        sdi[pidx(r)] = -(double)d.y;
+    }
+    __syncwarp();
+    const int R = P == 1 ? 32 : 64;
+    double Fr, Fi, Lr = 0, Li = 0;
+    const int f = lane * P, l = f + P - 1;
+    if (P == 1) {
+        Fr = sdr[pidx(f)];
+        Fi = sdi[pidx(f)];
+    } else {
+        for (int i = f + 2; i <= l; i++) {
+            double r = dn[i];
+            sdr[pidx(i)] += r * sdr[pidx(i - 1)];
+            sdi[pidx(i)] += r * sdi[pidx(i - 1)];
+        }
+        Lr = sdr[pidx(l)];
+        Li = sdi[pidx(l)];
+        for (int i = l - 2; i >= f + 1; i--) {
+            double r = up[i];
+            sdr[pidx(i)] += r * sdr[pidx(i + 1)];
+            sdi[pidx(i)] += r * sdi[pidx(i + 1)];
+        }
+        Fr = sdr[pidx(f)];
+        Fi = sdi[pidx(f)];
+        if (P >= 3) {
+            Fr += rF[lane] * sdr[pidx(f + 1)];
+            Fi += rF[lane] * sdi[pidx(f + 1)];
+        }
+    }
+    // cyclic reduction on the right-hand sides of the R boundary rows
+    // (row 2k = F, 2k+1 = L of lane k; one row per lane when R = 32)
+    int level = 0;
+    for (int s = 1; s < R; s <<= 1, level++) {
+        const double* L0 = pl + level * 64;
+        const double* H0 = ph + level * 64;
+        if (R == 32) {
+            double lr = __shfl_up_sync(0xffffffffu, Fr, s), li = __shfl_up_sync(0xffffffffu, Fi, s);
+            double hr = __shfl_down_sync(0xffffffffu, Fr, s), hi = __shfl_down_sync(0xffffffffu, Fi, s);
+            if (lane < s) lr = li = 0.0;
+            if (lane + s >= 32) hr = hi = 0.0;
+            Fr += L0[lane] * lr + H0[lane] * hr;
+            Fi += L0[lane] * li + H0[lane] * hi;
+            continue;
+        }
+        double lFr, lFi, hFr, hFi, lLr, lLi, hLr, hLi;  // neighbours of F (row 2k) and L (row 2k+1)
+        if (s == 1) {
+            lFr = __shfl_up_sync(0xffffffffu, Lr, 1);
+            lFi = __shfl_up_sync(0xffffffffu, Li, 1);
+            hLr = __shfl_down_sync(0xffffffffu, Fr, 1);
+            hLi = __shfl_down_sync(0xffffffffu, Fi, 1);
+            if (lane == 0) lFr = lFi = 0.0;
+            if (lane == 31) hLr = hLi = 0.0;
+            hFr = Lr;
+            hFi = Li;
+            lLr = Fr;
+            lLi = Fi;
+        } else {
+            const int t = s >> 1;
+            lFr = __shfl_up_sync(0xffffffffu, Fr, t);
+            lFi = __shfl_up_sync(0xffffffffu, Fi, t);
+            hFr = __shfl_down_sync(0xffffffffu, Fr, t);
+            hFi = __shfl_down_sync(0xffffffffu, Fi, t);
+            lLr = __shfl_up_sync(0xffffffffu, Lr, t);
+            lLi = __shfl_up_sync(0xffffffffu, Li, t);
+            hLr = __shfl_down_sync(0xffffffffu, Lr, t);
+            hLi = __shfl_down_sync(0xffffffffu, Li, t);
+            if (lane < t) lFr = lFi = lLr = lLi = 0.0;
+            if (lane + t >= 32) hFr = hFi = hLr = hLi = 0.0;
+        }
+        const int iF = 2 * lane, iL = iF + 1;
+        double nFr = Fr + L0[iF] * lFr + H0[iF] * hFr, nFi = Fi + L0[iF] * lFi + H0[iF] * hFi;
+        double nLr = Lr + L0[iL] * lLr + H0[iL] * hLr, nLi = Li + L0[iL] * lLi + H0[iL] * hLi;
+        Fr = nFr;
+        Fi = nFi;
+        Lr = nLr;
+        Li = nLi;
+    }
+    if (P == 1) {
+        double iv = pinv[lane];
+        sol[(size_t)f * n] = make_float2((float)(Fr * iv), (float)(Fi * iv));
+        return;
+    }
+    const double xfr = Fr * pinv[2 * lane], xfi = Fi * pinv[2 * lane];
+    const double xlr = Lr * pinv[2 * lane + 1], xli = Li * pinv[2 * lane + 1];
+    sol[(size_t)f * n] = make_float2((float)xfr, (float)xfi);
+    sol[(size_t)l * n] = make_float2((float)xlr, (float)xli);
+    for (int i = f + 1; i <= l - 1; i++) {
+        double iv = bInv[i];
+        double xr = (sdr[pidx(i)] + bA[i] * xfr + bC[i] * xlr) * iv;
+        double xi = (sdi[pidx(i)] + bA[i] * xfi + bC[i] * xli) * iv;
+        sol[(size_t)i * n] = make_float2((float)xr, (float)xi);
+    }
+}
+
+// Blocks [0, nfp64) solve modes 1..nfp64 in FP64 (warp 0), the rest one FP32
+// mode each.  P = nTheta / blockDim.x rows per thread for the FP32 modes.
+template <int P>
+__global__ void __launch_bounds__(SOLVE_THREADS) k_solve(KGeo g, KBufs b, int nfp64)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    if ((int)blockIdx.x < nfp64) {
+        if (threadIdx.x >= 32) return;
+        double* base = reinterpret_cast<double*>(smraw);
+        const int stride = g.nt + 32;
+        solve_mode64(g, b, blockIdx.x + 1, base, base + stride);
+        return;
+    }
+    solve_mode32<P>(g, b, (int)blockIdx.x + 1, reinterpret_cast<Row<float>*>(smraw));
+}
+
+// ---------------------------------------------------- inverse FFT + u update
+// p_j = sum_{m=1}^{nt-1} 2 Re(U_m e^{i m phi_j}) + U_nt (-1)^j: the m = 0
+// mode is never synthesised, which is exactly the reference's subtraction of
+// the cached zero component (cacheZeroComponents / shiftUKernel,
+// KaminoCore.cu:672-703).  Through a length-nt complex FFT of
+// Y_m = (X_m + X_{m+nt}) + i (X_m - X_{m+nt}) e^{i pi m/nt}, X the Hermitian
+// spectrum, whose output is z_k = p_{2k} + i p_{2k+1}.
+__global__ void __launch_bounds__(512) k_ifft_u(KGeo g, KBufs b, int uv_in, int uv_out, int write_p)
 {
     extern __shared__ float2 sm2[];
-    const int nt = g.nt, np = g.np, mask = g.mask;
-    const int r0 = blockIdx.x * FFT_ROWS;
-    const int nrows = min(FFT_ROWS + 1, nt - r0);
-    const int ld = nt + 1;
-    float2* U = sm2;                         // staged U_m, slot m % nt
-    float2* Fb = sm2 + (FFT_ROWS + 1) * ld;  // FFT rows
-    for (int t = threadIdx.x; t < nt * nrows; t += blockDim.x) {
-        int mi = t / nrows, r = t - mi * nrows;
-        U[r * ld + ((mi + 1) & (nt - 1))] = b.spec[(size_t)mi * nt + r0 + r];
-    }
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (warp < nrows) {
-        const float2* Ur = U + warp * ld;
-        float2* x = Fb + warp * ld;
-        // Y_m = (X_m + X_{m+nt}) + i (X_m - X_{m+nt}) e^{i pi m/nt} with
-        // X_0 = 0, X_m = U_m, X_{m+nt} = conj(U_{nt-m}); X_nt = U_nt (real).
-        for (int m = lane; m <= nt / 2; m += 32) {
-            if (m == 0) {
-                float un = Ur[0].x;
-                x[0] = make_float2(un, -un);
-                continue;
-            }
-            const int mb = nt - m;
-            float2 ua = Ur[m], ub = Ur[mb];
-            float2 ea = __ldg(b.rt + m), eb = __ldg(b.rt + mb);
-            {
-                float Er = ua.x + ub.x, Ei = ua.y - ub.y, Dr = ua.x - ub.x, Di = ua.y + ub.y;
-                float Or = Dr * ea.x + Di * ea.y, Oi = Di * ea.x - Dr * ea.y;  // D * conj(rt)
-                x[bitrev(m, g.log2nt)] = make_float2(Er - Oi, Ei + Or);
-            }
-            if (mb != m) {
-                float Er = ub.x + ua.x, Ei = ub.y - ua.y, Dr = ub.x - ua.x, Di = ub.y + ua.y;
-                float Or = Dr * eb.x + Di * eb.y, Oi = Di * eb.x - Dr * eb.y;
-                x[bitrev(mb, g.log2nt)] = make_float2(Er - Oi, Ei + Or);
-            }
+    const int N = g.nt, T = N >> 2, rpc = fft_rows_per_cta(N);
+    const int lr = threadIdx.x / T, t = threadIdx.x - lr * T;
+    const int j = blockIdx.x * rpc + lr;
+    const int np = g.np, mask = g.mask;
+    float2* bufA = sm2 + (size_t)lr * 2 * N;
+    float2* bufB = bufA + N;
+    const float2* __restrict__ U = b.sol + (size_t)j * N;  // U[m-1] = U_m
+    float2 v[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const int m = t + r * T;
+        if (m == 0) {
+            float un = __ldg(&U[N - 1].x);  // X_nt = U_nt, real
+            v[r] = make_float2(un, -un);
+            continue;
         }
-        __syncwarp();
-        fft_dit_warp<true>(x, nt, g.log2nt, b.tw, lane);
+        float2 ua = __ldg(U + m - 1), ub = __ldg(U + N - m - 1);  // X_m, and X_{m+nt} = conj(U_{nt-m})
+        float2 ea = __ldg(b.rt + m);
+        float Er = ua.x + ub.x, Ei = ua.y - ub.y, Dr = ua.x - ub.x, Di = ua.y + ub.y;
+        float Or = Dr * ea.x + Di * ea.y, Oi = Di * ea.x - Dr * ea.y;  // D * e^{+i pi m/nt}
+        v[r] = make_float2(Er - Oi, Ei + Or);
     }
-    __syncthreads();
+    const float2* Z = stockham<true>(v, bufA, bufB, N, t, b.tw);
+    const float* pr = reinterpret_cast<const float*>(Z);
     const float* __restrict__ uf = b.u[uv_in];
-    const float* __restrict__ vf = b.v[uv_in];
     float* __restrict__ uo = b.u[uv_out];
-    float* __restrict__ vo = b.v[uv_out];
-    const float* pr = reinterpret_cast<const float*>(Fb);
-    const int ldp = 2 * ld;
-    const float neg_h = -g.h;
-    for (int t = threadIdx.x; t < FFT_ROWS * np; t += blockDim.x) {
-        int r = t / np, i = t - r * np;
-        int j = r0 + r;
-        size_t gi = (size_t)j * np + i;
-        float pc = pr[r * ldp + i], pw = pr[r * ldp + ((i - 1) & mask)];
+    const float nhs = __ldg(b.negHs + j);
+    const size_t row = (size_t)j * np;
+    for (int i = t; i < np; i += T) {
+        float pc = pr[i], pw = pr[(i - 1) & mask];
         // applyPressurePhi, KaminoCore.cu:740-746
-        uo[gi] = __fadd_rn(__ldg(uf + gi), __fdiv_rn(__fsub_rn(pc, pw), __ldg(b.negHs + j)));
-        if (j < nt - 1) {
-            // applyPressureTheta, KaminoCore.cu:716-721
-            float ps = pr[(r + 1) * ldp + i];
-            vo[gi] = __fadd_rn(__ldg(vf + gi), __fdiv_rn(__fsub_rn(ps, pc), neg_h));
-        }
-        if (write_p) b.p[gi] = pc;
+        uo[row + i] = __fadd_rn(__ldg(uf + row + i), __fdiv_rn(__fsub_rn(pc, pw), nhs));
+        b.p[row + i] = pc;
     }
+    (void)write_p;
+}
+
+// applyPressureTheta (KaminoCore.cu:716-721): v -= (p[j+1] - p[j]) / h
+__global__ void __launch_bounds__(ELEM_THREADS) k_vgrad(KGeo g, KBufs b, int uv_in, int uv_out)
+{
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (g.nt - 1) * g.np) return;
+    float pn = __ldg(b.p + idx), ps = __ldg(b.p + idx + g.np);
+    b.v[uv_out][idx] = __fadd_rn(__ldg(b.v[uv_in] + idx), __fdiv_rn(__fsub_rn(ps, pn), -g.h));
 }
 
 // ------------------------------------------------------------- probes

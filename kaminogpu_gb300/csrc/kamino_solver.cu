@@ -58,9 +58,9 @@ struct kamino_solver_s {
     size_t smem_div = 0, smem_solve = 0, smem_ifft = 0;
 };
 
-static const char* const kKernelNames[] = {"k_advect", "k_geo_centers", "k_div_fft", "k_solve",
-                                           "k_ifft_grad"};
-static const int kNumKernels = 5;
+static const char* const kKernelNames[] = {"k_advect", "k_geo_centers", "k_div_fft",
+                                           "k_solve",  "k_ifft_u",      "k_vgrad"};
+static const int kNumKernels = 6;
 
 extern "C" const char* kamino_kernel_name(int index)
 {
@@ -90,8 +90,8 @@ static float pi_up_threshold()
 static int fill_geo(const kamino_config* c, KGeo* g)
 {
     const int nt = c->n_theta;
-    if (nt < 16 || nt > 2048 || (nt & (nt - 1)))
-        return kamino_fail(KAMINO_ERR_INVALID, "n_theta=%d: must be a power of two in [16, 2048]", nt);
+    if (nt < 32 || nt > 2048 || (nt & (nt - 1)))
+        return kamino_fail(KAMINO_ERR_INVALID, "n_theta=%d: must be a power of two in [32, 2048]", nt);
     if (!(c->radius > 0) || !std::isfinite(c->radius))
         return kamino_fail(KAMINO_ERR_INVALID, "radius=%g must be positive", c->radius);
     if (!(c->dt > 0) || !std::isfinite(c->dt))
@@ -110,6 +110,7 @@ static int fill_geo(const kamino_config* c, KGeo* g)
     g->R = (float)c->radius;
     g->dt = (float)c->dt;
     g->cofTheta = g->dt / g->R;
+    g->cellTheta = (float)(c->dt / (c->radius * (KAMINO_PI_D / nt)));
     g->pi_up = pi_up_threshold();
     g->wrap_phi_hi = wrap_threshold();
     g->pitch = g->np;
@@ -177,6 +178,86 @@ static void laplacian_rows(int nt, std::vector<double>& A, std::vector<double>& 
     }
 }
 
+// Multiplier tables of the FP64 mode solves (layout: kk::s64_stride).  The
+// device solve of a mode repeats the dominance-form elimination of
+// solve_mode32 on the right-hand side only; the matrix part is fixed per
+// sphere, so it is run here once, in double.
+static void fp64_tables(int nt, int nmodes, const std::vector<double>& A, const std::vector<double>& C,
+                        const std::vector<double>& S, std::vector<double>& out)
+{
+    const size_t stride = kk::s64_stride(nt);
+    out.assign(stride * (size_t)nmodes, 0.0);
+    const int P = nt >> 5;
+    struct R3 {
+        double a, c, s;
+    };
+    for (int q = 0; q < nmodes; q++) {
+        const double m2 = (double)(q + 1) * (q + 1);
+        double* tb = out.data() + stride * q;
+        double *dn = tb, *up = tb + nt, *bA = tb + 2 * nt, *bC = tb + 3 * nt, *bInv = tb + 4 * nt;
+        double *rF = tb + 5 * nt, *pl = rF + 32, *ph = pl + 6 * 64, *pinv = ph + 6 * 64;
+        std::vector<R3> red;
+        if (P == 1) {
+            for (int i = 0; i < nt; i++) red.push_back({A[i], C[i], m2 * S[i]});
+        } else {
+            std::vector<double> a(A), c(C), s(nt);
+            for (int i = 0; i < nt; i++) s[i] = m2 * S[i];
+            for (int k = 0; k < 32; k++) {
+                const int f = k * P, l = f + P - 1;
+                for (int i = f + 2; i <= l; i++) {  // downward
+                    double r = a[i] / (s[i - 1] + a[i - 1] + c[i - 1]);
+                    dn[i] = r;
+                    a[i] = r * a[i - 1];
+                    s[i] += r * s[i - 1];
+                }
+                R3 L = {a[l], c[l], s[l]};
+                if (P >= 3) {  // row l-1 starts the upward pass as it is
+                    bA[l - 1] = a[l - 1];
+                    bC[l - 1] = c[l - 1];
+                    bInv[l - 1] = 1.0 / (s[l - 1] + a[l - 1] + c[l - 1]);
+                }
+                for (int i = l - 2; i >= f + 1; i--) {  // upward
+                    double r = c[i] / (s[i + 1] + a[i + 1] + c[i + 1]);
+                    up[i] = r;
+                    a[i] += r * a[i + 1];
+                    c[i] = r * c[i + 1];
+                    s[i] += r * s[i + 1];
+                    bA[i] = a[i];
+                    bC[i] = c[i];
+                    bInv[i] = 1.0 / (s[i] + a[i] + c[i]);
+                }
+                R3 F = {a[f], c[f], s[f]};
+                if (P >= 3) {
+                    double r = c[f] / (s[f + 1] + a[f + 1] + c[f + 1]);
+                    rF[k] = r;
+                    F.c = r * c[f + 1];
+                    F.s += r * s[f + 1];
+                }
+                red.push_back(F);
+                red.push_back(L);
+            }
+        }
+        const int R = (int)red.size();
+        int level = 0;
+        for (int sft = 1; sft < R; sft <<= 1, level++) {
+            std::vector<R3> nx(R);
+            for (int i = 0; i < R; i++) {
+                R3 lo = i - sft >= 0 ? red[i - sft] : R3{0, 0, 1};
+                R3 hi = i + sft < R ? red[i + sft] : R3{0, 0, 1};
+                double rl = red[i].a / (lo.s + lo.a + lo.c), rh = red[i].c / (hi.s + hi.a + hi.c);
+                pl[level * 64 + i] = rl;
+                ph[level * 64 + i] = rh;
+                nx[i] = {rl * lo.a, rh * hi.c, red[i].s + rl * lo.s + rh * hi.s};
+            }
+            red = nx;
+        }
+        for (int i = 0; i < R; i++) pinv[i] = 1.0 / (red[i].s + red[i].a + red[i].c);
+    }
+}
+
+// FP32 rows per thread of k_solve and its block size.
+static int solve_rows(int nt) { return nt >= 256 ? nt / kk::SOLVE_THREADS : 1; }
+
 extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
 {
     if (!cfg || !out) return kamino_fail(KAMINO_ERR_INVALID, "kamino_create: null argument");
@@ -206,7 +287,8 @@ extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
     const size_t part = align_up(sizeof(float2) * (size_t)std::max<int64_t>(npart, 1));
     const size_t rowf = align_up(sizeof(float) * nt), rowd = align_up(sizeof(double) * nt);
     const size_t tw = align_up(sizeof(float2) * nt), rt = align_up(sizeof(float2) * (nt + 1));
-    size_t total = 9 * field + spec + 2 * part + 11 * rowf + 4 * rowd + tw + rt;
+    const size_t s64 = align_up(sizeof(double) * kk::s64_stride(nt) * std::max(h->nfp64, 1));
+    size_t total = 9 * field + 2 * spec + 2 * part + 13 * rowf + 4 * rowd + tw + rt + s64;
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&h->arena, total);
     if (e != cudaSuccess) {
@@ -232,8 +314,12 @@ extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
     b.cv = (float*)take(field);
     b.p = (float*)take(field);
     b.spec = (float2*)take(spec);
+    b.sol = (float2*)take(spec);
+    b.s64 = (double*)take(s64);
     b.cof_c = (float*)take(rowf);
     b.cof_v = (float*)take(rowf);
+    b.cell_c = (float*)take(rowf);
+    b.cell_v = (float*)take(rowf);
     b.gfac = (float*)take(rowf);
     b.negHs = (float*)take(rowf);
     b.divf = (float*)take(rowf);
@@ -268,6 +354,17 @@ extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
             double a = -KAMINO_PI_D * m / nt;
             rth[m] = make_float2((float)std::cos(a), (float)std::sin(a));
         }
+        // velocity -> displacement in cells, dt / (R sin(theta) h), exact h
+        std::vector<float> cellc(nt), cellv(nt);
+        {
+            const double hd = KAMINO_PI_D / nt;
+            for (int j = 0; j < nt; j++) {
+                cellc[j] = (float)(cfg->dt / (cfg->radius * std::sin((j + 0.5) * hd) * hd));
+                cellv[j] = (float)(cfg->dt / (cfg->radius * std::sin((j + 1.0) * hd) * hd));
+            }
+        }
+        std::vector<double> t64;
+        if (h->nfp64 > 0) fp64_tables(nt, h->nfp64, A, C, S, t64);
         struct {
             void* d;
             const void* s;
@@ -276,8 +373,11 @@ extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
                    {b.lapB0, B0f.data(), 4 * (size_t)nt},  {b.lapS, Sf.data(), 4 * (size_t)nt},
                    {b.lapA64, A.data(), 8 * (size_t)nt},   {b.lapC64, C.data(), 8 * (size_t)nt},
                    {b.lapB064, B0.data(), 8 * (size_t)nt}, {b.lapS64, S.data(), 8 * (size_t)nt},
-                   {b.tw, twh.data(), 8 * (size_t)nt},     {b.rt, rth.data(), 8 * (size_t)(nt + 1)}};
+                   {b.tw, twh.data(), 8 * (size_t)nt},     {b.rt, rth.data(), 8 * (size_t)(nt + 1)},
+                   {b.cell_c, cellc.data(), 4 * (size_t)nt}, {b.cell_v, cellv.data(), 4 * (size_t)nt},
+                   {b.s64, t64.data(), 8 * t64.size()}};
         for (auto& u : ups) {
+            if (!u.n) continue;
             e = cudaMemcpyAsync(u.d, u.s, u.n, cudaMemcpyHostToDevice, h->stream);
             if (e != cudaSuccess) break;
         }
@@ -287,18 +387,18 @@ extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
         if (e != cudaSuccess) break;
         e = cudaStreamSynchronize(h->stream);  // host vectors above go out of scope
         if (e != cudaSuccess) break;
-        h->smem_div = sizeof(float2) * kk::FFT_ROWS * (nt + 1);
-        h->smem_solve = (size_t)kk::SOLVE_WARPS * 4 * (nt + 32) * sizeof(float);
-        h->smem_ifft = sizeof(float2) * 2 * (kk::FFT_ROWS + 1) * (nt + 1);
+        const int rpc = kk::fft_rows_per_cta(nt);
+        h->smem_div = sizeof(float2) * 2 * (size_t)nt * rpc;
+        h->smem_ifft = h->smem_div;
+        const int P = solve_rows(nt);
+        const size_t red = sizeof(kk::Row<float>) * (P == 1 ? nt : 2 * (nt / P));
+        h->smem_solve = std::max(red, sizeof(double) * 2 * (size_t)(nt + 32));
         e = cudaFuncSetAttribute(kk::k_div_fft<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem_div);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(kk::k_div_fft<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)h->smem_div);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(kk::k_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)h->smem_solve);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(kk::k_ifft_grad, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            e = cudaFuncSetAttribute(kk::k_ifft_u, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)h->smem_ifft);
     } while (0);
     if (e != cudaSuccess) {
@@ -317,7 +417,12 @@ static int launch_advect(kamino_solver_s* h, int suv, int duv, int sr, int dr)
     const int T = kk::ADV_THREADS;
     int nb_u = (g.nt * g.np + T - 1) / T, nb_v = ((g.nt - 1) * g.np + T - 1) / T, nb_r = nb_u;
     int nb_p = (int)((h->b.npart + T - 1) / T);
-    kk::k_advect<<<nb_u + nb_v + nb_r + nb_p, T, 0, h->stream>>>(g, h->b, suv, duv, sr, dr, nb_u, nb_v, nb_r);
+    if (g.flags & KAMINO_F_REFERENCE_ROUNDING)
+        kk::k_advect<true><<<nb_u + nb_v + nb_r + nb_p, T, 0, h->stream>>>(g, h->b, suv, duv, sr, dr, nb_u, nb_v,
+                                                                           nb_r);
+    else
+        kk::k_advect<false><<<nb_u + nb_v + nb_r + nb_p, T, 0, h->stream>>>(g, h->b, suv, duv, sr, dr, nb_u, nb_v,
+                                                                            nb_r);
     return cudaGetLastError() == cudaSuccess ? KAMINO_OK : KAMINO_ERR_CUDA;
 }
 
@@ -325,7 +430,17 @@ static int launch_geo(kamino_solver_s* h, int src)
 {
     const KGeo& g = h->g;
     int n = g.nt * g.np;
-    kk::k_geo_centers<<<(n + 255) / 256, 256, 0, h->stream>>>(g, h->b, src);
+    kk::k_geo_centers<<<(n + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS, kk::ELEM_THREADS, 0, h->stream>>>(g, h->b,
+                                                                                                        src);
+    return cudaGetLastError() == cudaSuccess ? KAMINO_OK : KAMINO_ERR_CUDA;
+}
+
+static int launch_assign(kamino_solver_s* h, int uv_out)
+{
+    const KGeo& g = h->g;
+    int n = g.nt * g.np;
+    kk::k_assign<<<(n + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS, kk::ELEM_THREADS, 0, h->stream>>>(g, h->b,
+                                                                                                   uv_out);
     return cudaGetLastError() == cudaSuccess ? KAMINO_OK : KAMINO_ERR_CUDA;
 }
 
@@ -333,31 +448,41 @@ template <int MODE>
 static int launch_div(kamino_solver_s* h, int uv_in, int uv_out)
 {
     const KGeo& g = h->g;
-    kk::k_div_fft<MODE><<<g.nt / kk::FFT_ROWS, 32 * kk::FFT_ROWS, MODE == 1 ? 0 : h->smem_div, h->stream>>>(
-        g, h->b, uv_in, uv_out);
+    const int rpc = kk::fft_rows_per_cta(g.nt);
+    kk::k_div_fft<MODE><<<g.nt / rpc, rpc * (g.nt / 4), h->smem_div, h->stream>>>(g, h->b, uv_in, uv_out);
     return cudaGetLastError() == cudaSuccess ? KAMINO_OK : KAMINO_ERR_CUDA;
 }
 
 static int launch_solve(kamino_solver_s* h)
 {
     const KGeo& g = h->g;
-    int n32 = g.nt - h->nfp64;
-    int grid = h->nfp64 + (n32 + kk::SOLVE_WARPS - 1) / kk::SOLVE_WARPS;
-    kk::k_solve<<<grid, 32 * kk::SOLVE_WARPS, h->smem_solve, h->stream>>>(g, h->b, h->nfp64);
+    const int P = solve_rows(g.nt), threads = g.nt / P;
+    const int grid = g.nt;  // blocks [0, nfp64) take the FP64 modes
+    switch (P) {
+    case 1: kk::k_solve<1><<<grid, threads, h->smem_solve, h->stream>>>(g, h->b, h->nfp64); break;
+    case 2: kk::k_solve<2><<<grid, threads, h->smem_solve, h->stream>>>(g, h->b, h->nfp64); break;
+    case 4: kk::k_solve<4><<<grid, threads, h->smem_solve, h->stream>>>(g, h->b, h->nfp64); break;
+    case 8: kk::k_solve<8><<<grid, threads, h->smem_solve, h->stream>>>(g, h->b, h->nfp64); break;
+    case 16: kk::k_solve<16><<<grid, threads, h->smem_solve, h->stream>>>(g, h->b, h->nfp64); break;
+    default: return KAMINO_ERR_INVALID;
+    }
     return cudaGetLastError() == cudaSuccess ? KAMINO_OK : KAMINO_ERR_CUDA;
 }
 
 static int launch_ifft(kamino_solver_s* h, int uv_in, int uv_out)
 {
     const KGeo& g = h->g;
-    int wp = (g.flags & KAMINO_F_NO_PRESSURE_OUT) ? 0 : 1;
-    kk::k_ifft_grad<<<g.nt / kk::FFT_ROWS, 32 * (kk::FFT_ROWS + 1), h->smem_ifft, h->stream>>>(g, h->b, uv_in,
-                                                                                              uv_out, wp);
+    const int rpc = kk::fft_rows_per_cta(g.nt);
+    kk::k_ifft_u<<<g.nt / rpc, rpc * (g.nt / 4), h->smem_ifft, h->stream>>>(g, h->b, uv_in, uv_out, 1);
+    if (cudaGetLastError() != cudaSuccess) return KAMINO_ERR_CUDA;
+    int n = (g.nt - 1) * g.np;
+    kk::k_vgrad<<<(n + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS, kk::ELEM_THREADS, 0, h->stream>>>(g, h->b, uv_in,
+                                                                                                  uv_out);
     return cudaGetLastError() == cudaSuccess ? KAMINO_OK : KAMINO_ERR_CUDA;
 }
 
 // The fused step from parity (cu, cr); ev, when given, receives an external
-// event record before the first and after every kernel (6 events).
+// event record before the first and after every kernel (kNumKernels + 1).
 static int enqueue_step(kamino_solver_s* h, int cu, int cr, cudaEvent_t* ev)
 {
     int rc = 0;
@@ -373,8 +498,21 @@ static int enqueue_step(kamino_solver_s* h, int cu, int cr, cudaEvent_t* ev)
     mark(3);
     rc |= launch_solve(h);
     mark(4);
-    rc |= launch_ifft(h, cu, 1 - cu);
+    {
+        const KGeo& g = h->g;
+        const int rpc = kk::fft_rows_per_cta(g.nt);
+        kk::k_ifft_u<<<g.nt / rpc, rpc * (g.nt / 4), h->smem_ifft, h->stream>>>(g, h->b, cu, 1 - cu, 1);
+        rc |= cudaGetLastError() == cudaSuccess ? 0 : KAMINO_ERR_CUDA;
+    }
     mark(5);
+    {
+        const KGeo& g = h->g;
+        int n = (g.nt - 1) * g.np;
+        kk::k_vgrad<<<(n + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS, kk::ELEM_THREADS, 0, h->stream>>>(g, h->b, cu,
+                                                                                                      1 - cu);
+        rc |= cudaGetLastError() == cudaSuccess ? 0 : KAMINO_ERR_CUDA;
+    }
+    mark(6);
     return rc ? kamino_fail(KAMINO_ERR_CUDA, "kernel launch failed: %s",
                             cudaGetErrorString(cudaGetLastError()))
               : KAMINO_OK;
@@ -487,7 +625,7 @@ extern "C" int kamino_geometric(kamino_handle h)
     int rc = check_handle(h);
     if (rc) return rc;
     rc = launch_geo(h, h->cur_uv);
-    if (!rc) rc = launch_div<1>(h, h->cur_uv, 1 - h->cur_uv);
+    if (!rc) rc = launch_assign(h, 1 - h->cur_uv);
     if (rc) return kamino_fail(rc, "geometric launch: %s", cudaGetErrorString(cudaGetLastError()));
     h->cur_uv ^= 1;
     return KAMINO_OK;
@@ -669,7 +807,7 @@ extern "C" int kamino_time_kernels(kamino_handle h, int reps, int flush_l2, doub
     if (reps <= 0 || !ms) return kamino_fail(KAMINO_ERR_INVALID, "bad arguments");
     if (flush_l2 && (rc = ensure_flush(h))) return rc;
     std::vector<double> acc(kNumKernels, 0.0);
-    cudaEvent_t ev[2][6];
+    cudaEvent_t ev[2][kNumKernels + 1];
     for (auto& row : ev)
         for (auto& e : row) KCUDA(cudaEventCreate(&e));
     // one graph per parity, each with event nodes around every kernel

@@ -164,14 +164,16 @@ static void swapp(double **a, double **b)
 }
 
 /* ------------------------------------------------------------- lifecycle */
-oracle *oracle_create(int nt, double R, double dt, unsigned flags, int64_t npart)
+/* h <= 0 selects the exact spacing pi/nTheta; a positive h (e.g. the float
+ * gridLenGlobal of the reference) is used as given. */
+oracle *oracle_create_h(int nt, double R, double dt, unsigned flags, int64_t npart, double h_in)
 {
     if (nt < 4 || (nt & (nt - 1))) return NULL;
     oracle *o = (oracle *)calloc(1, sizeof(oracle));
     o->nt = nt;
     o->np = 2 * nt;
     o->mask = o->np - 1;
-    o->h = O_PI / nt;
+    o->h = h_in > 0 ? h_in : O_PI / nt;
     o->R = R;
     o->dt = dt;
     o->flags = flags;
@@ -230,6 +232,11 @@ oracle *oracle_create(int nt, double R, double dt, unsigned flags, int64_t npart
     }
     o->spec = zalloc(2 * (size_t)nt * nt);
     return o;
+}
+
+oracle *oracle_create(int nt, double R, double dt, unsigned flags, int64_t npart)
+{
+    return oracle_create_h(nt, R, dt, flags, npart, 0.0);
 }
 
 void oracle_destroy(oracle *o)

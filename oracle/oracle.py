@@ -38,6 +38,8 @@ def _oracle_lib():
         L = ctypes.CDLL(ORACLE_SO)
         L.oracle_create.restype = _P
         L.oracle_create.argtypes = [_I, _D, _D, ctypes.c_uint, _I64]
+        L.oracle_create_h.restype = _P
+        L.oracle_create_h.argtypes = [_I, _D, _D, ctypes.c_uint, _I64, _D]
         L.oracle_destroy.argtypes = [_P]
         for f in ("oracle_advection", "oracle_geometric", "oracle_projection"):
             getattr(L, f).argtypes = [_P]
@@ -66,11 +68,11 @@ def grid_h(nt):
 class Oracle:
     """FP64 restatement of the reference step on one sphere."""
 
-    def __init__(self, nt, radius=1.0, dt=0.005, flags=0, n_particles=0):
+    def __init__(self, nt, radius=1.0, dt=0.005, flags=0, n_particles=0, h=0.0):
         self.L = _oracle_lib()
         self.nt, self.np_ = nt, 2 * nt
         self.n_particles = n_particles
-        self.o = self.L.oracle_create(nt, radius, dt, flags, n_particles)
+        self.o = self.L.oracle_create_h(nt, radius, dt, flags, n_particles, float(h))
         if not self.o:
             raise ValueError("oracle_create(nt=%d) failed" % nt)
 

@@ -11,7 +11,7 @@ from points import index_points
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("nt", [16, 64, 1024])
+@pytest.mark.parametrize("nt", [32, 64, 1024])
 @pytest.mark.parametrize("kind", [0, 1, 2])
 def test_index_map_bit_exact_vs_oracle(kg, orc, nt, kind):
     phi, theta = index_points(nt)
@@ -25,7 +25,7 @@ def test_index_map_bit_exact_vs_oracle(kg, orc, nt, kind):
     assert np.array_equal(ga.view(np.uint32), wa.view(np.uint32))
 
 
-@pytest.mark.parametrize("nt", [16, 128, 1024])
+@pytest.mark.parametrize("nt", [32, 128, 1024])
 @pytest.mark.parametrize("kind", [0, 1, 2])
 def test_index_map_bit_exact_vs_reference_kernels(kg, orc, nt, kind):
     if not orc.have_reference_gpu():

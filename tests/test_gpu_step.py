@@ -1,7 +1,12 @@
-"""Step parity on the GPU: each stage and whole steps of the CUDA solver
-against the FP64 oracle (relative L2 <= 1e-5 per field, the north-star
-tolerance) and against the reference's own kernels run on the same inputs
-(post-projection divergence within 2x)."""
+"""Step parity on the GPU.
+
+* Default (cell-exact) sampler: each stage and whole steps against the FP64
+  oracle, relative L2 <= 1e-5 per field after 1 and 100 steps.
+* Reference-rounding sampler (KAMINO_F_REFERENCE_ROUNDING): against the
+  reference's own kernels run on the same inputs; never worse than the
+  reference's own FP32 error against FP64, post-projection divergence within
+  2x of the reference's.
+"""
 import numpy as np
 import pytest
 
@@ -16,15 +21,15 @@ def make_pair(kg, orc, nt, dt, lmax=8, seed=3, npart=0, flags=0, vortex=False, f
     cfg = kg.default_config(n_theta=nt, radius=1.0, dt=dt, n_particles=npart, flags=flags, fp64_modes=fp64_modes)
     s = kg.KaminoSolver(config=cfg)
     s.load(st)
-    o = orc.Oracle(nt, 1.0, dt, flags, npart)
+    o = orc.Oracle(nt, 1.0, dt, flags & 3, npart)
     o.load(st)
     return st, s, o
 
 
-@pytest.mark.parametrize("nt", [32, 128])
+@pytest.mark.parametrize("nt", [32, 128, 1024])
 @pytest.mark.parametrize("stage", ["advection", "geometric", "projection"])
 def test_stage_vs_fp64_oracle(kg, orc, nt, stage):
-    st, s, o = make_pair(kg, orc, nt, 0.005)
+    st, s, o = make_pair(kg, orc, nt, 0.005 if nt < 1024 else 0.001, lmax=8 if nt < 1024 else 32)
     getattr(s, stage)()
     getattr(o, stage)()
     got, want = s.fields(), o.fields()
@@ -35,9 +40,10 @@ def test_stage_vs_fp64_oracle(kg, orc, nt, stage):
 
 
 @pytest.mark.parametrize("nt,dt,steps,lmax", [(32, 0.005, 1, 8), (32, 0.005, 100, 8), (128, 0.005, 1, 8),
-                                              (128, 0.005, 100, 8), (256, 0.002, 20, 16)])
+                                              (128, 0.005, 100, 8), (256, 0.002, 100, 16),
+                                              (1024, 0.001, 1, 32)])
 def test_step_vs_fp64_oracle(kg, orc, nt, dt, steps, lmax):
-    st, s, o = make_pair(kg, orc, nt, dt, lmax=lmax)
+    st, s, o = make_pair(kg, orc, nt, dt, lmax=lmax, vortex=nt >= 1024)
     s.step_n(steps)
     o.step(steps)
     got, want = s.fields(), o.fields()
@@ -47,9 +53,10 @@ def test_step_vs_fp64_oracle(kg, orc, nt, dt, steps, lmax):
         assert err <= TOL, "%s after %d steps (nt=%d): rel L2 %.3e" % (k, steps, nt, err)
 
 
-def test_stages_compose_to_step_bitwise(kg, orc):
+@pytest.mark.parametrize("flags", [0, 16])
+def test_stages_compose_to_step_bitwise(kg, orc, flags):
     st = kg.make_initial_state(64, lmax=8, seed=5, n_particles=4096)
-    cfg = kg.default_config(n_theta=64, radius=1.0, dt=0.005, n_particles=4096)
+    cfg = kg.default_config(n_theta=64, radius=1.0, dt=0.005, n_particles=4096, flags=flags)
     with kg.KaminoSolver(config=cfg) as a, kg.KaminoSolver(config=cfg) as b:
         a.load(st)
         b.load(st)
@@ -64,11 +71,11 @@ def test_stages_compose_to_step_bitwise(kg, orc):
 
 
 @pytest.mark.parametrize("nt", [32, 128])
-def test_step_vs_reference_kernels(kg, orc, nt):
+def test_reference_rounding_step_vs_reference_kernels(kg, orc, nt):
     if not orc.have_reference_gpu():
         pytest.skip("reference cubins not built")
     dt = 0.005
-    st, s, o = make_pair(kg, orc, nt, dt, npart=1024)
+    st, s, o = make_pair(kg, orc, nt, dt, npart=1024, flags=kg.F_REFERENCE_ROUNDING)
     ref = orc.RefGPU(nt, 1.0, dt, 1024)
     ref.load(st)
     s.stepForward()
@@ -86,9 +93,34 @@ def test_step_vs_reference_kernels(kg, orc, nt):
     d_ours = np.linalg.norm(o.divergence(got["u_phi"], got["u_theta"]))
     d_ref = np.linalg.norm(o.divergence(rf["u_phi"], rf["u_theta"]))
     assert 0.5 <= d_ours / d_ref <= 2.0, (d_ours, d_ref)
-    # particles: same forward-Euler update (KaminoCore.cu:321-342)
+    # particles: the same forward-Euler update (KaminoCore.cu:321-342)
     dp = np.abs(got["particles"].astype(np.float64) - rf["particles"]).max()
     assert dp < 1e-5, dp
+
+
+@pytest.mark.parametrize("nt", [128, 1024])
+def test_divergence_within_2x_of_reference(kg, orc, nt):
+    """Default sampler: post-projection divergence is at most 2x the reference
+    kernels' on the same input, and within 1% of the FP64 oracle's.  (At
+    nTheta = 1024 the reference's own FP32 cyclic reduction leaves a
+    divergence ~1000x the FP64 one, so "within 2x" is one-sided there.)"""
+    if not orc.have_reference_gpu():
+        pytest.skip("reference cubins not built")
+    dt = 0.005 if nt < 1024 else 0.001
+    st, s, o = make_pair(kg, orc, nt, dt, lmax=8 if nt < 1024 else 32)
+    ref = orc.RefGPU(nt, 1.0, dt)
+    ref.load(st)
+    s.stepForward()
+    ref.step(1)
+    o.step(1)
+    got, rf = s.fields(), ref.fields()
+    s.close()
+    ref.close()
+    d_ours = np.linalg.norm(o.divergence(got["u_phi"], got["u_theta"]))
+    d_ref = np.linalg.norm(o.divergence(rf["u_phi"], rf["u_theta"]))
+    d_fp64 = np.linalg.norm(o.divergence())
+    assert d_ours <= 2.0 * d_ref, (d_ours, d_ref)
+    assert abs(d_ours / d_fp64 - 1.0) < 1e-2, (d_ours, d_fp64)
 
 
 def test_particles_vs_fp64_oracle(kg, orc):
@@ -101,3 +133,16 @@ def test_particles_vs_fp64_oracle(kg, orc):
         d = np.abs(gp - wp)
         d[:, 0] = np.minimum(d[:, 0], 2 * np.pi - d[:, 0])  # phi is periodic
         assert np.percentile(d, 99.9) < 1e-4, (flags, np.percentile(d, 99.9))
+
+
+@pytest.mark.parametrize("fp64_modes", [0, 4, 16])
+def test_fp64_mode_solves_agree(kg, orc, fp64_modes):
+    """FP64 low-mode solves and the FP32 dominance-form solves give the same
+    projection within the FP32 right-hand-side limit."""
+    st, s, o = make_pair(kg, orc, 256, 0.002, lmax=16, fp64_modes=fp64_modes)
+    s.projection()
+    o.projection()
+    got, want = s.fields(), o.fields()
+    s.close()
+    for k in ("u_phi", "u_theta"):
+        assert orc.rel_l2(got[k], want[k]) <= TOL, (k, orc.rel_l2(got[k], want[k]))
