@@ -163,6 +163,23 @@ int kamino_advection(kamino_handle h);
 int kamino_geometric(kamino_handle h);
 int kamino_projection(kamino_handle h);
 
+/* Pressure projection of caller-owned fields that allocates no device memory.
+ * No counterpart in the reference.  It is for callers that cannot call
+ * cudaMalloc (code running inside another framework's memory pool, or whose
+ * device memory is fixed at start-up): they pass device pointers to the
+ * input and output fields, and the projection's temporaries live in one
+ * fixed 1.25 MiB array compiled into the library, which every GPU that loads
+ * the library holds until exit.  Limit: n_theta a power of two in [32, 256];
+ * larger sizes return KAMINO_ERR_INVALID.  Modes |m| <= 4 are solved in FP64.
+ * Dense rows of 2*n_theta floats: u_phi / u_phi_out n_theta rows, u_theta /
+ * u_theta_out n_theta-1 rows, pressure_out n_theta rows (outputs may alias
+ * inputs).  stream is a cudaStream_t (NULL: the default stream); the call is
+ * asynchronous on it.  The first call on a device looks up the array's
+ * device address, so make it before any stream capture on that device.  All
+ * calls share the array: calls whose work overlaps on the GPU race. */
+int kamino_projection_noalloc(int n_theta, const float* u_phi, const float* u_theta, float* u_phi_out,
+                              float* u_theta_out, float* pressure_out, void* stream);
+
 /* n steps of the configured dt, replayed from CUDA graphs. */
 int kamino_step_n(kamino_handle h, int n);
 

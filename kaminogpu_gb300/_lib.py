@@ -118,6 +118,7 @@ SIGNATURES = {
     "kamino_geometric": (_I, [_P]),
     "kamino_projection": (_I, [_P]),
     "kamino_step_n": (_I, [_P, _I]),
+    "kamino_projection_noalloc": (_I, [_I, _P, _P, _P, _P, _P, _P]),
     "kamino_run_frames": (_I, [_P, _I, ctypes.POINTER(_I64)]),
     "kamino_synchronize": (_I, [_P]),
     "kamino_time_elapsed": (_I, [_P, ctypes.POINTER(_D), ctypes.POINTER(_I64)]),

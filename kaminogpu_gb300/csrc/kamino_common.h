@@ -15,6 +15,15 @@ int kamino_fail(int code, const char* fmt, ...)
 #endif
     ;
 
+#ifdef __cplusplus
+#include <vector>
+// Host tables shared by the solver units (kamino_solver.cu).
+void laplacian_rows(int nt, std::vector<double>& A, std::vector<double>& C, std::vector<double>& B0,
+                    std::vector<double>& S);
+void fp64_tables(int nt, int nmodes, const std::vector<double>& A, const std::vector<double>& C,
+                 const std::vector<double>& S, std::vector<double>& out);
+#endif
+
 #define KAMINO_PI_D 3.14159265358979323846   /* M_PI  (KaminoHeader.cuh:26) */
 #define KAMINO_2PI_D 6.28318530717958647692  /* M_2PI (KaminoHeader.cuh:27) */
 

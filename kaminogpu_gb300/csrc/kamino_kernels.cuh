@@ -23,6 +23,9 @@
 #include "kamino_device.cuh"
 
 namespace kk {
+// internal linkage: every translation unit that launches these kernels
+// compiles its own copy
+namespace {
 
 using namespace kdev;
 
@@ -693,4 +696,5 @@ __global__ void k_probe_wrap(KGeo g, float* phi, float* theta, int64_t n, int* c
     cells[2 * k + 1] = (int)floorf(__fdiv_rn(t, g.h));
 }
 
+} // namespace
 } // namespace kk

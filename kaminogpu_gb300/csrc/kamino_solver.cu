@@ -150,8 +150,8 @@ extern "C" int kamino_destroy(kamino_handle h)
 
 // Laplacian rows of precomputeABCKernel (KaminoSolver.cu:128-159) for n != 0,
 // with h = pi/nTheta in double: B(n) = B0 - n^2 * S.
-static void laplacian_rows(int nt, std::vector<double>& A, std::vector<double>& C, std::vector<double>& B0,
-                           std::vector<double>& S)
+void laplacian_rows(int nt, std::vector<double>& A, std::vector<double>& C, std::vector<double>& B0,
+                    std::vector<double>& S)
 {
     const double h = KAMINO_PI_D / nt;
     A.resize(nt);
@@ -182,8 +182,8 @@ static void laplacian_rows(int nt, std::vector<double>& A, std::vector<double>& 
 // device solve of a mode repeats the dominance-form elimination of
 // solve_mode32 on the right-hand side only; the matrix part is fixed per
 // sphere, so it is run here once, in double.
-static void fp64_tables(int nt, int nmodes, const std::vector<double>& A, const std::vector<double>& C,
-                        const std::vector<double>& S, std::vector<double>& out)
+void fp64_tables(int nt, int nmodes, const std::vector<double>& A, const std::vector<double>& C,
+                 const std::vector<double>& S, std::vector<double>& out)
 {
     const size_t stride = kk::s64_stride(nt);
     out.assign(stride * (size_t)nmodes, 0.0);
