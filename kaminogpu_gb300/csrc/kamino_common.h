@@ -24,6 +24,19 @@ void fp64_tables(int nt, int nmodes, const std::vector<double>& A, const std::ve
                  const std::vector<double>& S, std::vector<double>& out);
 #endif
 
+// Internal hooks for the batched and served forms (kamino_batch.cu): they
+// advance many handles with shared launches and keep each handle's
+// bookkeeping (buffer parity, step count) in step.
+struct KGeo;
+struct KBufs;
+int kamino_internal_desc(kamino_handle h, KGeo* g, KBufs* b, int* nfp64, int* cur_uv, int* cur_r);
+int kamino_internal_advance(kamino_handle h, int nsteps);
+int kamino_internal_get_counters(kamino_handle h, int* cur_uv, int* cur_r, int64_t* steps, double* time);
+int kamino_internal_set_counters(kamino_handle h, int cur_uv, int cur_r, int64_t steps, double time);
+// Re-targets a handle of the same nTheta to a new radius / dt / flags and
+// zeroes its state, so pooled device memory can serve a new request.
+int kamino_internal_reset(kamino_handle h, const kamino_config* cfg);
+
 #define KAMINO_PI_D 3.14159265358979323846   /* M_PI  (KaminoHeader.cuh:26) */
 #define KAMINO_2PI_D 6.28318530717958647692  /* M_2PI (KaminoHeader.cuh:27) */
 

@@ -88,21 +88,21 @@ __device__ __forceinline__ void advect_particle(const KGeo& g, const float* __re
     out = make_float2(updatedPhi, updatedTheta);
 }
 
-// Blocks [0, nb_u) advect u_phi, then u_theta, then thickness, then
-// particles; each thread one grid point or one particle.  REF selects the
-// reference-rounding (radian) sampler, otherwise the cell-exact one.
+// Tile `blk` of the advection: tiles [0, nb_u) advect u_phi, then u_theta,
+// then thickness, then particles, ADV_THREADS points each; thread `tid` one
+// grid point or one particle.  REF selects the reference-rounding (radian)
+// sampler, otherwise the cell-exact one.
 template <bool REF>
-__global__ void __launch_bounds__(ADV_THREADS) k_advect(KGeo g, KBufs b, int suv, int duv, int sr, int dr,
-                                                         int nb_u, int nb_v, int nb_r)
+__device__ __forceinline__ void advect_tile(const KGeo& g, const KBufs& b, int suv, int duv, int sr, int dr,
+                                            int nb_u, int nb_v, int nb_r, int blk, int tid)
 {
     const float* __restrict__ u = b.u[suv];
     const float* __restrict__ v = b.v[suv];
-    int blk = blockIdx.x;
     const int lg = g.log2nt + 1;  // log2(nPhi)
     if (blk < nb_u + nb_v + nb_r) {
         const int which = blk < nb_u ? 0 : (blk < nb_u + nb_v ? 1 : 2);
         const int b0 = which == 0 ? 0 : (which == 1 ? nb_u : nb_u + nb_v);
-        int idx = (blk - b0) * ADV_THREADS + threadIdx.x;
+        int idx = (blk - b0) * ADV_THREADS + tid;
         if (idx >= (which == 1 ? g.nt - 1 : g.nt) * g.np) return;
         int j = idx >> lg, i = idx & g.mask;
         float val;
@@ -130,17 +130,23 @@ __global__ void __launch_bounds__(ADV_THREADS) k_advect(KGeo g, KBufs b, int suv
         return;
     }
     blk -= nb_u + nb_v + nb_r;
-    int64_t k = (int64_t)blk * ADV_THREADS + threadIdx.x;
+    int64_t k = (int64_t)blk * ADV_THREADS + tid;
     if (k >= b.npart) return;
     float2 out;
     advect_particle(g, u, v, b.part[sr][k], out);
     b.part[dr][k] = out;
 }
 
-// --------------------------------------------------------------- geometric
-__global__ void __launch_bounds__(ELEM_THREADS) k_geo_centers(KGeo g, KBufs b, int src)
+template <bool REF>
+__global__ void __launch_bounds__(ADV_THREADS) k_advect(KGeo g, KBufs b, int suv, int duv, int sr, int dr,
+                                                         int nb_u, int nb_v, int nb_r)
 {
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    advect_tile<REF>(g, b, suv, duv, sr, dr, nb_u, nb_v, nb_r, blockIdx.x, threadIdx.x);
+}
+
+// --------------------------------------------------------------- geometric
+__device__ __forceinline__ void geo_tile(const KGeo& g, const KBufs& b, int src, int idx)
+{
     if (idx >= g.nt * g.np) return;
     const int lg = g.log2nt + 1;
     int j = idx >> lg, i = idx & g.mask;
@@ -159,6 +165,11 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_geo_centers(KGeo g, KBufs b, i
     float vNext = __fadd_rn(vPrev, __fmul_rn(__fmul_rn(G, uNext), uNext));
     b.cu[idx] = uNext;
     b.cv[idx] = vNext;
+}
+
+__global__ void __launch_bounds__(ELEM_THREADS) k_geo_centers(KGeo g, KBufs b, int src)
+{
+    geo_tile(g, b, src, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // assignPhiKernel / assignThetaKernel (KaminoCore.cu:517-549) alone, for the
@@ -249,13 +260,14 @@ __host__ __device__ inline int fft_rows_per_cta(int nt) { return nt >= 1024 ? 1 
 // MODE 2: from face velocities (projection stage called by itself)
 // Writes c_m = (1/nPhi) sum_j div_j e^{-i m phi_j}, m = 1..nt, mode-major:
 // spec[(m-1)*nt + row].  c_0 (the dropped m = 0 mode) is never formed.
+// Tile `blk` = rows [blk*rpc, blk*rpc + rpc) with rpc*N/4 threads.
 template <int MODE>
-__global__ void __launch_bounds__(512) k_div_fft(KGeo g, KBufs b, int uv_in, int uv_out)
+__device__ __forceinline__ void div_fft_tile(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int blk,
+                                             int tid, float2* sm2)
 {
-    extern __shared__ float2 sm2[];
     const int N = g.nt, T = N >> 2, rpc = fft_rows_per_cta(N);
-    const int lr = threadIdx.x / T, t = threadIdx.x - lr * T;
-    const int j = blockIdx.x * rpc + lr;
+    const int lr = tid / T, t = tid - lr * T;
+    const int j = blk * rpc + lr;
     const int np = g.np, mask = g.mask;
     float2* bufA = sm2 + (size_t)lr * 2 * N;
     float2* bufB = bufA + N;
@@ -322,6 +334,13 @@ __global__ void __launch_bounds__(512) k_div_fft(KGeo g, KBufs b, int uv_in, int
     }
 }
 
+template <int MODE>
+__global__ void __launch_bounds__(512) k_div_fft(KGeo g, KBufs b, int uv_in, int uv_out)
+{
+    extern __shared__ float2 sm2[];
+    div_fft_tile<MODE>(g, b, uv_in, uv_out, blockIdx.x, threadIdx.x, sm2);
+}
+
 // ------------------------------------------------------------- mode solve
 // Each Fourier mode m >= 1 of the pressure solves the reference's tridiagonal
 // system (precomputeABCKernel, KaminoSolver.cu:128-159; crKernel, tdm.cu)
@@ -363,16 +382,20 @@ __device__ __forceinline__ Row<float> pcr_combine(const Row<float>& x, const Row
 }
 
 // Shared-memory PCR over R rows (R a power of two); thread t owns rows
-// t*q .. t*q+q-1, q = R / nthreads (1 or 2).
+// t*Q .. t*Q+Q-1.  Every thread of the CTA calls it (it synchronises);
+// threads with active == false own no rows.
 template <int Q>
-__device__ __forceinline__ void pcr_smem(Row<float> (&r)[Q], Row<float>* rs, int R, int t)
+__device__ __forceinline__ void pcr_smem(Row<float> (&r)[Q], Row<float>* rs, int R, int t, bool active)
 {
     for (int s = 1; s < R; s <<= 1) {
+        if (active) {
 #pragma unroll
-        for (int e = 0; e < Q; e++) rs[t * Q + e] = r[e];
+            for (int e = 0; e < Q; e++) rs[t * Q + e] = r[e];
+        }
         __syncthreads();
 #pragma unroll
         for (int e = 0; e < Q; e++) {
+            if (!active) break;
             const int i = t * Q + e;
             Row<float> lo, hi;
             if (i - s >= 0) {
@@ -393,25 +416,32 @@ __device__ __forceinline__ void pcr_smem(Row<float> (&r)[Q], Row<float>* rs, int
     }
 }
 
-// FP32 solve of mode m by the whole CTA (blockDim.x = nt / P threads).
+// FP32 solve of mode m by one CTA: thread t owns rows [t P, t P + P).  With
+// P == 1 the CTA may be wider than nt (threads t >= nt only synchronise);
+// with P >= 2 it has exactly nt / P threads.
 template <int P>
-__device__ void solve_mode32(const KGeo& g, const KBufs& b, int m, Row<float>* rs)
+__device__ void solve_mode32(const KGeo& g, const KBufs& b, int m, Row<float>* rs, int t)
 {
-    const int n = g.nt, t = threadIdx.x;
+    const int n = g.nt;
     const float m2 = (float)m * (float)m;
     const float2* __restrict__ col = b.spec + (size_t)(m - 1) * n;
     float2* __restrict__ sol = b.sol + (m - 1);  // sol[row * n + m - 1]
     if (P == 1) {
+        const bool active = t < n;
         Row<float> r[1];
-        r[0].a = __ldg(b.lapA + t);
-        r[0].c = __ldg(b.lapC + t);
-        r[0].s = m2 * __ldg(b.lapS + t);
-        float2 d = col[t];
-        r[0].dr = -d.x;
-        r[0].di = -d.y;
-        pcr_smem<1>(r, rs, n, t);
-        float inv = rcpf(r[0].s + r[0].a + r[0].c);
-        sol[(size_t)t * n] = make_float2(r[0].dr * inv, r[0].di * inv);
+        if (active) {
+            r[0].a = __ldg(b.lapA + t);
+            r[0].c = __ldg(b.lapC + t);
+            r[0].s = m2 * __ldg(b.lapS + t);
+            float2 d = col[t];
+            r[0].dr = -d.x;
+            r[0].di = -d.y;
+        }
+        pcr_smem<1>(r, rs, n, t, active);
+        if (active) {
+            float inv = rcpf(r[0].s + r[0].a + r[0].c);
+            sol[(size_t)t * n] = make_float2(r[0].dr * inv, r[0].di * inv);
+        }
         return;
     }
     const int f = t * P;
@@ -462,7 +492,7 @@ __device__ void solve_mode32(const KGeo& g, const KBufs& b, int m, Row<float>* r
         rr[0].dr += r * Dr[1];
         rr[0].di += r * Di[1];
     }
-    pcr_smem<2>(rr, rs, 2 * blockDim.x, t);
+    pcr_smem<2>(rr, rs, 2 * (n / P), t, true);
     float iF = rcpf(rr[0].s + rr[0].a + rr[0].c), iL = rcpf(rr[1].s + rr[1].a + rr[1].c);
     const float xfr = rr[0].dr * iF, xfi = rr[0].di * iF, xlr = rr[1].dr * iL, xli = rr[1].di * iL;
     sol[(size_t)f * n] = make_float2(xfr, xfi);
@@ -590,8 +620,28 @@ __device__ void solve_mode64(const KGeo& g, const KBufs& b, int m, double* sdr, 
     }
 }
 
-// Blocks [0, nfp64) solve modes 1..nfp64 in FP64 (warp 0), the rest one FP32
-// mode each.  P = nTheta / blockDim.x rows per thread for the FP32 modes.
+// Mode blk + 1: FP64 (warp 0) when blk < nfp64, otherwise FP32 with P rows
+// per thread (P is a runtime value here; the batched kernels mix sizes).
+__device__ __forceinline__ void solve_tile_p(const KGeo& g, const KBufs& b, int nfp64, int blk, int tid,
+                                             unsigned char* smraw, int P)
+{
+    if (blk < nfp64) {  // FP64 mode, warp 0; the other threads have nothing to do
+        if (tid >= 32) return;
+        double* base = reinterpret_cast<double*>(smraw);
+        const int stride = g.nt + 32;
+        solve_mode64(g, b, blk + 1, base, base + stride);
+        return;
+    }
+    Row<float>* rs = reinterpret_cast<Row<float>*>(smraw);
+    switch (P) {
+    case 1: solve_mode32<1>(g, b, blk + 1, rs, tid); break;
+    case 2: solve_mode32<2>(g, b, blk + 1, rs, tid); break;
+    case 4: solve_mode32<4>(g, b, blk + 1, rs, tid); break;
+    case 8: solve_mode32<8>(g, b, blk + 1, rs, tid); break;
+    default: solve_mode32<16>(g, b, blk + 1, rs, tid); break;
+    }
+}
+
 template <int P>
 __global__ void __launch_bounds__(SOLVE_THREADS) k_solve(KGeo g, KBufs b, int nfp64)
 {
@@ -603,7 +653,7 @@ __global__ void __launch_bounds__(SOLVE_THREADS) k_solve(KGeo g, KBufs b, int nf
         solve_mode64(g, b, blockIdx.x + 1, base, base + stride);
         return;
     }
-    solve_mode32<P>(g, b, (int)blockIdx.x + 1, reinterpret_cast<Row<float>*>(smraw));
+    solve_mode32<P>(g, b, (int)blockIdx.x + 1, reinterpret_cast<Row<float>*>(smraw), threadIdx.x);
 }
 
 // ---------------------------------------------------- inverse FFT + u update
@@ -613,12 +663,12 @@ __global__ void __launch_bounds__(SOLVE_THREADS) k_solve(KGeo g, KBufs b, int nf
 // KaminoCore.cu:672-703).  Through a length-nt complex FFT of
 // Y_m = (X_m + X_{m+nt}) + i (X_m - X_{m+nt}) e^{i pi m/nt}, X the Hermitian
 // spectrum, whose output is z_k = p_{2k} + i p_{2k+1}.
-__global__ void __launch_bounds__(512) k_ifft_u(KGeo g, KBufs b, int uv_in, int uv_out, int write_p)
+__device__ __forceinline__ void ifft_tile(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int blk, int tid,
+                                          float2* sm2)
 {
-    extern __shared__ float2 sm2[];
     const int N = g.nt, T = N >> 2, rpc = fft_rows_per_cta(N);
-    const int lr = threadIdx.x / T, t = threadIdx.x - lr * T;
-    const int j = blockIdx.x * rpc + lr;
+    const int lr = tid / T, t = tid - lr * T;
+    const int j = blk * rpc + lr;
     const int np = g.np, mask = g.mask;
     float2* bufA = sm2 + (size_t)lr * 2 * N;
     float2* bufB = bufA + N;
@@ -650,16 +700,26 @@ __global__ void __launch_bounds__(512) k_ifft_u(KGeo g, KBufs b, int uv_in, int 
         uo[row + i] = __fadd_rn(__ldg(uf + row + i), __fdiv_rn(__fsub_rn(pc, pw), nhs));
         b.p[row + i] = pc;
     }
+}
+
+__global__ void __launch_bounds__(512) k_ifft_u(KGeo g, KBufs b, int uv_in, int uv_out, int write_p)
+{
+    extern __shared__ float2 sm2[];
+    ifft_tile(g, b, uv_in, uv_out, blockIdx.x, threadIdx.x, sm2);
     (void)write_p;
 }
 
 // applyPressureTheta (KaminoCore.cu:716-721): v -= (p[j+1] - p[j]) / h
-__global__ void __launch_bounds__(ELEM_THREADS) k_vgrad(KGeo g, KBufs b, int uv_in, int uv_out)
+__device__ __forceinline__ void vgrad_tile(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int idx)
 {
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (g.nt - 1) * g.np) return;
     float pn = __ldg(b.p + idx), ps = __ldg(b.p + idx + g.np);
     b.v[uv_out][idx] = __fadd_rn(__ldg(b.v[uv_in] + idx), __fdiv_rn(__fsub_rn(ps, pn), -g.h));
+}
+
+__global__ void __launch_bounds__(ELEM_THREADS) k_vgrad(KGeo g, KBufs b, int uv_in, int uv_out)
+{
+    vgrad_tile(g, b, uv_in, uv_out, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ------------------------------------------------------------- probes

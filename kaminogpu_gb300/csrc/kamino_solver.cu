@@ -666,6 +666,89 @@ extern "C" int kamino_synchronize(kamino_handle h)
     return KAMINO_OK;
 }
 
+// ------------------------------------------------------------ internal hooks
+int kamino_internal_desc(kamino_handle h, KGeo* g, KBufs* b, int* nfp64, int* cur_uv, int* cur_r)
+{
+    if (!h) return kamino_fail(KAMINO_ERR_INVALID, "null handle");
+    if (g) *g = h->g;
+    if (b) *b = h->b;
+    if (nfp64) *nfp64 = h->nfp64;
+    if (cur_uv) *cur_uv = h->cur_uv;
+    if (cur_r) *cur_r = h->cur_r;
+    return KAMINO_OK;
+}
+
+int kamino_internal_advance(kamino_handle h, int nsteps)
+{
+    if (!h) return kamino_fail(KAMINO_ERR_INVALID, "null handle");
+    if (nsteps & 1) {
+        h->cur_uv ^= 1;
+        h->cur_r ^= 1;
+    }
+    h->steps += nsteps;
+    h->time += (double)h->g.dt * nsteps;
+    return KAMINO_OK;
+}
+
+int kamino_internal_get_counters(kamino_handle h, int* cur_uv, int* cur_r, int64_t* steps, double* time)
+{
+    if (!h) return kamino_fail(KAMINO_ERR_INVALID, "null handle");
+    if (cur_uv) *cur_uv = h->cur_uv;
+    if (cur_r) *cur_r = h->cur_r;
+    if (steps) *steps = h->steps;
+    if (time) *time = h->time;
+    return KAMINO_OK;
+}
+
+int kamino_internal_set_counters(kamino_handle h, int cur_uv, int cur_r, int64_t steps, double time)
+{
+    if (!h) return kamino_fail(KAMINO_ERR_INVALID, "null handle");
+    h->cur_uv = cur_uv & 1;
+    h->cur_r = cur_r & 1;
+    h->steps = steps;
+    h->time = time;
+    return KAMINO_OK;
+}
+
+int kamino_internal_reset(kamino_handle h, const kamino_config* cfg)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!cfg || cfg->n_theta != h->g.nt)
+        return kamino_fail(KAMINO_ERR_INVALID, "reset needs a config with the same n_theta");
+    KGeo g;
+    rc = fill_geo(cfg, &g);
+    if (rc) return rc;
+    if (kamino_particle_count(cfg) != h->b.npart)
+        return kamino_fail(KAMINO_ERR_INVALID, "reset needs the same particle count");
+    h->cfg = *cfg;
+    h->g = g;
+    h->cur_uv = h->cur_r = 0;
+    h->steps = 0;
+    h->time = 0.0;
+    h->last_dt = g.dt;
+    destroy_graphs(h);
+    const int nt = g.nt;
+    std::vector<float> cellc(nt), cellv(nt);
+    const double hd = KAMINO_PI_D / nt;
+    for (int j = 0; j < nt; j++) {
+        cellc[j] = (float)(cfg->dt / (cfg->radius * std::sin((j + 0.5) * hd) * hd));
+        cellv[j] = (float)(cfg->dt / (cfg->radius * std::sin((j + 1.0) * hd) * hd));
+    }
+    const size_t field = sizeof(float) * (size_t)g.rows * g.np;
+    for (int s = 0; s < 2; s++) {
+        KCUDA(cudaMemsetAsync(h->b.u[s], 0, field, h->stream));
+        KCUDA(cudaMemsetAsync(h->b.v[s], 0, field, h->stream));
+        KCUDA(cudaMemsetAsync(h->b.rho[s], 0, field, h->stream));
+    }
+    KCUDA(cudaMemcpyAsync(h->b.cell_c, cellc.data(), 4 * (size_t)nt, cudaMemcpyHostToDevice, h->stream));
+    KCUDA(cudaMemcpyAsync(h->b.cell_v, cellv.data(), 4 * (size_t)nt, cudaMemcpyHostToDevice, h->stream));
+    kk::k_tables<<<(nt + 127) / 128, 128, 0, h->stream>>>(h->g, h->b);
+    KCUDA(cudaGetLastError());
+    KCUDA(cudaStreamSynchronize(h->stream));
+    return KAMINO_OK;
+}
+
 extern "C" int kamino_time_elapsed(kamino_handle h, double* t, int64_t* steps)
 {
     if (!h) return kamino_fail(KAMINO_ERR_INVALID, "null handle");

@@ -1,0 +1,133 @@
+"""The oracle (test infrastructure) pinned before it is trusted:
+* its FFT/solve/synthesis against numpy's FFT and a dense solve,
+* its reference-arithmetic index map against an independent numpy
+  restatement, and bit-exact against the reference's own validateCoord run
+  on a GB300 (tests/golden/ref_index.npz, made by make_golden.py),
+* its FP64 stages and steps against the reference's own kernels' outputs
+  (tests/golden/ref_step.npz) within the reference's FP32 error."""
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_projection_solves_the_reference_mode_systems(kg, orc):
+    """p satisfies A U_{i-1} + B U_i + C U_{i+1} = c_m for every m >= 1
+    (precomputeABCKernel, KaminoSolver.cu:128-159), c_m = rfft(div)/nPhi."""
+    nt, npp = 32, 64
+    rng = np.random.default_rng(0)
+    u = rng.standard_normal((nt, npp)).astype(np.float32)
+    v = rng.standard_normal((nt - 1, npp)).astype(np.float32)
+    o = orc.Oracle(nt)
+    o.set_state(0, u)
+    o.set_state(1, v)
+    div = o.divergence()
+    o.projection()
+    p = o.get_state(3)
+    h = np.pi / nt
+    th = (np.arange(nt) + 0.5) * h
+    P = np.fft.rfft(p, axis=1) / npp
+    c = np.fft.rfft(div, axis=1) / npp
+    for m in range(1, nt + 1):
+        A = 1 / h ** 2 - np.cos(th) / 2 / h / np.sin(th)
+        C = 1 / h ** 2 + np.cos(th) / 2 / h / np.sin(th)
+        B = -2 / h ** 2 - m * m / np.sin(th) ** 2
+        B[0] += A[0]
+        A[0] = 0
+        B[-1] += C[-1]
+        C[-1] = 0
+        x = P[:, m]
+        lhs = B * x
+        lhs[1:] += A[1:] * x[:-1]
+        lhs[:-1] += C[:-1] * x[1:]
+        assert np.abs(lhs - c[:, m]).max() <= 1e-10 * np.abs(c[:, m]).max(), m
+    assert np.abs(p.mean(axis=1)).max() < 1e-12  # the m = 0 mode is dropped
+
+
+def np_ref_index(kind, phi, theta, nt):
+    """Independent restatement of KaminoCore.cu:38-52 with numpy scalars."""
+    f32, f64 = np.float32, np.float64
+    h = f32(np.pi / nt)
+    offp = (-0.5, 0.0, 0.0)[kind]
+    offt = (0.5, 1.0, 0.5)[kind]
+    out = np.zeros((len(phi), 4), np.int64)
+    for k in range(len(phi)):
+        p = f32(f64(phi[k]) - f64(h) * offp)
+        t = f32(f64(theta[k]) - f64(h) * offt)
+        ret = f32(1)
+        t = f32(f64(t) - int(np.floor(f32(f64(t) / (2 * np.pi)))) * (2 * np.pi))
+        if f64(t) > np.pi:
+            t = f32(2 * np.pi - f64(t))
+            p = f32(f64(p) + np.pi)
+            ret = -ret
+        if t < 0:
+            t = -t
+            p = f32(f64(p) + np.pi)
+            ret = -ret
+        p = f32(f64(p) - int(np.floor(f32(f64(p) / (2 * np.pi)))) * (2 * np.pi))
+        inv = f32(1.0 / f64(h))
+        ip, it = int(np.floor(f32(p * inv))), int(np.floor(f32(t * inv)))
+        pole_row = nt - 2 if kind == 1 else nt - 1
+        out[k] = (ip % (2 * nt), it, ret == -1, (it == 0 and ret == -1) or it == pole_row)
+    return out
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2])
+def test_ref_index_restatement_matches_numpy(orc, kind):
+    from points import index_points
+    phi, theta = index_points(64, n_random=3000, seed=kind)
+    sel = np.random.default_rng(kind).choice(len(phi), 6000, replace=False)
+    got, _ = orc.ref_index(kind, phi[sel], theta[sel], 64)
+    want = np_ref_index(kind, phi[sel], theta[sel], 64)
+    assert np.array_equal(got.astype(np.int64), want)
+
+
+def _golden(name):
+    path = os.path.join(GOLDEN, name)
+    if not os.path.exists(path):
+        pytest.fail("golden file %s missing; run tests/golden/make_golden.py on a GPU" % path)
+    return np.load(path)
+
+
+@pytest.mark.parametrize("nt", [32, 1024])
+def test_ref_index_bit_exact_vs_reference_validatecoord(orc, nt):
+    g = _golden("ref_index.npz")
+    phi, theta = g["phi_%d" % nt], g["theta_%d" % nt]
+    for kind in (0, 1, 2):
+        got, _ = orc.ref_index(kind, phi, theta, nt)
+        assert np.array_equal(got, g["index_%d_%d" % (nt, kind)]), kind
+    p, t, c = orc.ref_wrap(phi, theta, nt)
+    assert np.array_equal(p.view(np.uint32), g["wrap_phi_%d" % nt].view(np.uint32))
+    assert np.array_equal(t.view(np.uint32), g["wrap_theta_%d" % nt].view(np.uint32))
+    assert np.array_equal(c, g["cells_%d" % nt])
+
+
+@pytest.mark.parametrize("nt", [32, 64])
+def test_fp64_oracle_vs_reference_kernels(orc, nt):
+    """The FP64 restatement against the reference's FP32 kernels: equal up to
+    the reference's own FP32 rounding (rel. L2 <= 1e-3 per field)."""
+    g = _golden("ref_step.npz")
+    pre = "nt%d_" % nt
+    nt_, dt, npart, seed = g[pre + "meta"]
+    st = {k: g[pre + "in_" + k] for k in ("u_phi", "u_theta", "thickness", "particles")}
+    for stage in ("advection", "geometric", "projection"):
+        o = orc.Oracle(nt, 1.0, dt, 0, int(npart))
+        o.load(st)
+        getattr(o, stage)()
+        f = o.fields()
+        for k in ("u_phi", "u_theta", "thickness"):
+            err = orc.rel_l2(g[pre + stage + "_" + k], f[k])
+            assert err <= 1e-3, (stage, k, err)
+    for n in (1, 3):
+        o = orc.Oracle(nt, 1.0, dt, 0, int(npart))
+        o.load(st)
+        o.step(n)
+        f = o.fields()
+        for k in ("u_phi", "u_theta", "thickness"):
+            err = orc.rel_l2(g[pre + "step%d_" % n + k], f[k])
+            assert err <= 1e-3, (n, k, err)
+        d = np.abs(g[pre + "step%d_particles" % n].astype(np.float64) - f["particles"])
+        d[:, 0] = np.minimum(d[:, 0], 2 * np.pi - d[:, 0])
+        assert np.percentile(d, 99) < 1e-4, (n, np.percentile(d, 99))
