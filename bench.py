@@ -247,24 +247,221 @@ def run_ours(args, ws, rank, local, dist):
         "dominant_kernel": dom,
         "clocks": ck.summary(),
     }
+    if not args.no_batched:
+        out["batched"] = bench_batched(kg, local)
+    if not args.no_served:
+        out["served"] = bench_served(kg, local, args.served_seconds)
     if not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(st, samples=1)
+        out["cpu_baseline"] = cpu_baseline(st, seconds=10.0)
     return out
 
 
-def cpu_baseline(st, samples=1):
-    """The oracle's FP64 CPU step on a bounded sample: `samples` steps of the
-    same sphere, all host threads."""
+def _same(a, b):
+    import numpy as np
+    return all(np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)) for k in ("u_phi", "u_theta", "thickness"))
+
+
+def bench_batched(kg, local, n_spheres=256, steps=500):
+    """256 independent spheres, nTheta ~ U{32,64,128,256}, radius ~ U(0.5, 2),
+    dt 0.005, own l<=8 stream function each, FP64 modes |m|<=4: the batched
+    step (one persistent kernel per stage, one graph per step, autotuned)
+    against looping the plain solver over the same spheres."""
+    import numpy as np
+    from kaminogpu_gb300.batch import Batch
+    rng = np.random.default_rng(4)
+    nts = rng.choice([32, 64, 128, 256], n_spheres)
+    rads = rng.uniform(0.5, 2.0, n_spheres)
+    cfgs = [kg.default_config(n_theta=int(n), radius=float(r), dt=0.005, fp64_modes=4, device=local)
+            for n, r in zip(nts, rads)]
+    states = [kg.make_initial_state(int(n), lmax=8, seed=1000 + i, radius=float(r))
+              for i, (n, r) in enumerate(zip(nts, rads))]
+    cells = int(sum(int(n) * 2 * int(n) for n in nts))
+    b = Batch(cfgs)
+    for i, st in enumerate(states):
+        b.load(i, st)
+    tuned = b.autotune(reps=3)
+    for i, st in enumerate(states):
+        b.load(i, st)
+    b.step_n(3)
+    b.synchronize()
+    for i, st in enumerate(states):
+        b.load(i, st)
+    b.synchronize()
+    with Clocks(local) as ck:
+        t0 = time.perf_counter()
+        b.step_n(steps)
+        b.synchronize()
+        wall_batched = time.perf_counter() - t0
+    batched_out = [{"u_phi": None} for _ in states]
+    check_idx = list(range(0, n_spheres, 17))
+    for i in check_idx:
+        batched_out[i] = {"u_phi": b.get_state(i, kg.U_PHI), "u_theta": b.get_state(i, kg.U_THETA),
+                          "thickness": b.get_state(i, kg.THICKNESS)}
+    ms_dev = b.time_steps(20, flush_l2=False)
+    b.close()
+
+    solvers = [kg.KaminoSolver(config=c) for c in cfgs]
+    for s, st in zip(solvers, states):
+        s.load(st)
+        s.step_n(3)
+    for s in solvers:
+        s.synchronize()
+    # plain, as one simulation is run: step a sphere, wait, next sphere
+    for s, st in zip(solvers, states):
+        s.load(st)
+    t0 = time.perf_counter()
+    for s in solvers:
+        s.step_n(steps)
+        s.synchronize()
+    wall_sync = time.perf_counter() - t0
+    bitwise = all(_same(batched_out[i], solvers[i].fields()) for i in check_idx)
+    # plain, every sphere's stream queued before one wait at the end
+    for s, st in zip(solvers, states):
+        s.load(st)
+    for s in solvers:
+        s.synchronize()
+    t0 = time.perf_counter()
+    for s in solvers:
+        s.step_n(steps)
+    for s in solvers:
+        s.synchronize()
+    wall_async = time.perf_counter() - t0
+    for s in solvers:
+        s.close()
+    v_b = cells * steps / wall_batched
+    v_s = cells * steps / wall_sync
+    v_a = cells * steps / wall_async
+    return {"workload": "%d spheres, nTheta~U{32,64,128,256}, radius~U(0.5,2), dt=0.005, l<=8, fp64_modes=4, "
+                        "%d steps" % (n_spheres, steps),
+            "cells_per_step": cells, "value": v_b, "unit": UNIT, "wall_s": wall_batched,
+            "device_ms_per_step": ms_dev / 20, "autotuned": tuned,
+            "plain_loop_sync": {"value": v_s, "wall_s": wall_sync},
+            "plain_loop_async": {"value": v_a, "wall_s": wall_async},
+            "speedup_vs_plain": v_b / max(v_s, v_a),
+            "bitwise_equal_to_plain": bitwise, "spheres_compared": len(check_idx),
+            "clocks": ck.summary()}
+
+
+def served_requests(n, seed=5):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    nts = 2 ** rng.integers(6, 11, n)  # log-uniform over {64, ..., 1024}
+    steps = rng.integers(10, 501, n)
+    return [(int(a), int(b)) for a, b in zip(nts, steps)]
+
+
+def bench_served(kg, local, seconds, rate=200.0, budget=120 << 30):
+    """Requests of one sphere each: nTheta log-uniform over {64..1024},
+    steps ~ U[10, 500], dt 0.002, l<=16, FP64 modes |m|<=4, 120 GB budget.
+    closed loop: a fixed request set drained as fast as possible, against the
+    plain solver run per request (one cached handle per nTheta).  open loop:
+    Poisson arrivals at 200/s for `seconds`, p50/p99 latency."""
+    import numpy as np
+    from kaminogpu_gb300.batch import Server
+    init = {}
+
+    def state(nt, seed):
+        k = (nt, seed % 8)
+        if k not in init:
+            init[k] = kg.make_initial_state(nt, lmax=16, seed=2000 + seed % 8)
+        return init[k]
+
+    def cfg(nt):
+        return kg.default_config(n_theta=nt, radius=1.0, dt=0.002, fp64_modes=4, device=local)
+
+    out = {"workload": "requests: nTheta log-uniform {64..1024}, steps~U[10,500], dt=0.002, l<=16, fp64_modes=4, "
+                       "120 GB admission budget"}
+    # closed loop
+    reqs = served_requests(120)
+    cs_total = sum(nt * 2 * nt * st for nt, st in reqs)
+    srv = Server(budget_bytes=budget, steps_per_round=16, device=local)
+    for i, (nt, st) in enumerate(reqs[:5]):  # warm the handle pool
+        srv.submit(cfg(nt), state(nt, i), 3)
+    while srv.stats()["completed"] < 5:
+        srv.poll()
+    srv.close()
+    srv = Server(budget_bytes=budget, steps_per_round=16, device=local)
+    with Clocks(local) as ck:
+        t0 = time.perf_counter()
+        rids = [srv.submit(cfg(nt), state(nt, i), st) for i, (nt, st) in enumerate(reqs)]
+        done = 0
+        while done < len(reqs):
+            done += srv.poll()
+        wall_srv = time.perf_counter() - t0
+    stats = srv.stats()
+    served_res = {i: srv.fetch(rids[i]) for i in range(0, len(reqs), 13)}
+    srv.close()
+    handles = {}
+    for nt in sorted({nt for nt, _ in reqs}):
+        handles[nt] = kg.KaminoSolver(config=cfg(nt))
+        handles[nt].load(state(nt, 0))
+        handles[nt].step_n(3)
+        handles[nt].synchronize()
+    t0 = time.perf_counter()
+    bitwise = True
+    for i, (nt, st) in enumerate(reqs):
+        s = handles[nt]
+        s.load(state(nt, i))
+        s.step_n(st)
+        f = s.fields()
+        if i in served_res:
+            bitwise = bitwise and _same(served_res[i], f)
+    wall_plain = time.perf_counter() - t0
+    for s in handles.values():
+        s.close()
+    out["closed_loop"] = {"requests": len(reqs), "cell_steps": cs_total, "value": cs_total / wall_srv,
+                          "unit": UNIT, "wall_s": wall_srv, "p50_latency_s": stats["p50_latency_s"],
+                          "p99_latency_s": stats["p99_latency_s"],
+                          "plain_per_request": {"value": cs_total / wall_plain, "wall_s": wall_plain},
+                          "speedup_vs_plain": wall_plain / wall_srv, "bitwise_equal_to_plain": bitwise,
+                          "requests_compared": len(served_res), "clocks": ck.summary()}
+    # open loop: Poisson arrivals
+    rng = np.random.default_rng(6)
+    n_open = int(rate * seconds)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_open))
+    oreqs = served_requests(n_open, seed=7)
+    srv = Server(budget_bytes=budget, steps_per_round=16, device=local)
+    t_start = srv.now()
+    submitted = 0
+    done = 0
+    while done < n_open:
+        now = srv.now() - t_start
+        while submitted < n_open and arrivals[submitted] <= now:
+            nt, st = oreqs[submitted]
+            srv.submit(cfg(nt), state(nt, submitted), st, arrival=t_start + arrivals[submitted])
+            submitted += 1
+        done += srv.poll()
+        if submitted < n_open and srv.stats()["resident"] == 0:
+            time.sleep(max(0.0, min(0.001, arrivals[submitted] - (srv.now() - t_start))))
+    wall = srv.now() - t_start
+    s = srv.stats()
+    srv.close()
+    cs = sum(nt * 2 * nt * st for nt, st in oreqs)
+    out["open_loop"] = {"rate_per_s": rate, "arrival_window_s": float(arrivals[-1]), "requests": n_open,
+                        "cell_steps": cs, "value": cs / wall, "unit": UNIT, "wall_s": wall,
+                        "offered_cell_steps_per_s": cs / float(arrivals[-1]),
+                        "p50_latency_s": s["p50_latency_s"], "p99_latency_s": s["p99_latency_s"],
+                        "mean_latency_s": s["mean_latency_s"], "peak_resident_bytes": s["peak_resident_bytes"]}
+    return out
+
+
+def cpu_baseline(st, seconds=10.0):
+    """The oracle's FP64 CPU step on a bounded sample: as many steps of the
+    same sphere as fit in about `seconds`, all host threads."""
     from oracle import oracle as orc
     cores = orc.set_threads(os.cpu_count() or 1)
     o = orc.Oracle(NT, 1.0, DT)
     o.load(st)
     t0 = time.perf_counter()
+    o.step(1)
+    t1 = time.perf_counter() - t0
+    samples = int(max(1, min(500, seconds / max(t1, 1e-3))))
+    t0 = time.perf_counter()
     o.step(samples)
     dt = time.perf_counter() - t0
     o.close()
     return {"value": NT * 2 * NT * samples / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d FP64 step(s) of the nTheta=1024 sphere (%.1f s)" % (samples, dt)}
+            "sample": "%d FP64 steps of the nTheta=1024 sphere after 1 untimed (%.1f s)" % (samples, dt)}
 
 
 def run_reference(args, ws, rank):
@@ -276,11 +473,16 @@ def run_reference(args, ws, rank):
     cores = orc.set_threads(os.cpu_count() or 1)
     o = orc.Oracle(NT, 1.0, DT)
     o.load(st)
-    o.step(1)  # warm-up
     t0 = time.perf_counter()
-    o.step(args.steps)
+    o.step(1)  # warm-up
+    t1 = time.perf_counter() - t0
+    # a bounded sample: at most about 30 s of CPU work
+    n = int(max(1, min(args.steps, 30.0 / max(t1, 1e-3))))
+    t0 = time.perf_counter()
+    o.step(n)
     dt = time.perf_counter() - t0
-    value = NT * 2 * NT * args.steps / dt
+    args.steps = n
+    value = NT * 2 * NT * n / dt
     out = {
         "impl": "reference",
         "metric": METRIC,
@@ -322,10 +524,13 @@ def run_reference(args, ws, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--served-seconds", type=float, default=5.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

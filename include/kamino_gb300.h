@@ -173,7 +173,7 @@ int kamino_projection(kamino_handle h);
  * larger sizes return KAMINO_ERR_INVALID.  Modes |m| <= 4 are solved in FP64.
  * Dense rows of 2*n_theta floats: u_phi / u_phi_out n_theta rows, u_theta /
  * u_theta_out n_theta-1 rows, pressure_out n_theta rows (outputs may alias
- * inputs).  stream is a cudaStream_t (NULL: the default stream); the call is
+ * inputs); every pointer 16-byte aligned.  stream is a cudaStream_t (NULL: the default stream); the call is
  * asynchronous on it.  The first call on a device looks up the array's
  * device address, so make it before any stream capture on that device.  All
  * calls share the array: calls whose work overlaps on the GPU race. */

@@ -39,7 +39,7 @@ struct KSphere {
     KGeo g;
     KBufs b;
     int nb_u, nb_v, nb_r, nb_adv;  // advection tiles (u_phi, u_theta, thickness, all incl. particles)
-    int nb_elem;                   // 256-point tiles of nt * nPhi
+    int nb_elem;                   // tiles of ELEM_THREADS four-cell groups of nt * nPhi
     int nb_fft;                    // row groups of the FFT kernels
     int P;                         // solve rows per thread
     int nfp64;
@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(kk::ELEM_THREADS) kb_geo(const KSphere* __rest
     }
 }
 
-__global__ void __launch_bounds__(256) kb_div_fft(const KSphere* __restrict__ sph, const int2* __restrict__ items,
+__global__ void __launch_bounds__(1024) kb_div_fft(const KSphere* __restrict__ sph, const int2* __restrict__ items,
                                                   int n, int* counter, int uv_in, int uv_out)
 {
     extern __shared__ float2 sm2[];
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(kk::SOLVE_THREADS) kb_solve(const KSphere* __r
         kk::solve_tile_p(s.g, s.b, s.nfp64, w.y, threadIdx.x, smraw, s.P);
 }
 
-__global__ void __launch_bounds__(256) kb_ifft(const KSphere* __restrict__ sph, const int2* __restrict__ items,
+__global__ void __launch_bounds__(1024) kb_ifft(const KSphere* __restrict__ sph, const int2* __restrict__ items,
                                                int n, int* counter, int uv_in, int uv_out)
 {
     extern __shared__ float2 sm2[];
@@ -172,6 +172,7 @@ struct Engine {
     int n_items[ST_COUNT] = {};
     size_t item_off[ST_COUNT] = {};
     size_t smem_fft = 0, smem_solve = 0;
+    int fft_block = 256;  // threads of the FFT kernels: the largest sphere's fft_threads
     Shapes shapes;
     int cu = 0, cr = 0;
     cudaGraphExec_t graph[2][2] = {};
@@ -238,13 +239,11 @@ struct Engine {
             }
             if (s.g.nt > 1024) return kamino_fail(KAMINO_ERR_INVALID, "batched spheres need n_theta <= 1024");
             const int T = kk::ADV_THREADS;
-            s.nb_u = (s.g.nt * s.g.np + T - 1) / T;
-            s.nb_v = ((s.g.nt - 1) * s.g.np + T - 1) / T;
-            s.nb_r = s.nb_u;
+            kk::adv_tiles(s.g, s.nb_u, s.nb_v, s.nb_r);
             s.nb_adv = s.nb_u + s.nb_v + s.nb_r + (int)((s.b.npart + T - 1) / T);
-            s.nb_elem = (s.g.nt * s.g.np + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS;
+            s.nb_elem = (kk::elem_groups(s.g.nt * s.g.np) + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS;
             s.nb_fft = s.g.nt / kk::fft_rows_per_cta(s.g.nt);
-            s.P = s.g.nt >= 256 ? s.g.nt / kk::SOLVE_THREADS : 1;
+            s.P = kk::solve_rows(s.g.nt);
             s.ref = (s.g.flags & KAMINO_F_REFERENCE_ROUNDING) ? 1 : 0;
             host_desc.push_back(s);
             cells += (int64_t)s.g.nt * s.g.np;
@@ -292,15 +291,17 @@ struct Engine {
         // dynamic shared memory: largest sphere decides
         smem_fft = 0;
         smem_solve = 0;
+        fft_block = 32;
         for (const KSphere& s : host_desc) {
-            const int nt = s.g.nt, rpc = kk::fft_rows_per_cta(nt);
-            smem_fft = std::max(smem_fft, sizeof(float2) * 2 * (size_t)nt * rpc);
-            size_t red = sizeof(kk::Row<float>) * (s.P == 1 ? nt : 2 * (nt / s.P));
-            smem_solve = std::max(smem_solve, std::max(red, sizeof(double) * 2 * (size_t)(nt + 32)));
+            const int nt = s.g.nt;
+            smem_fft = std::max(smem_fft, kk::fft_smem(nt));
+            smem_solve = std::max(smem_solve, kk::solve_smem(nt));
+            fft_block = std::max(fft_block, kk::fft_threads(nt));
         }
-        BCUDA(cudaFuncSetAttribute(kb_div_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_fft));
-        BCUDA(cudaFuncSetAttribute(kb_ifft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_fft));
-        BCUDA(cudaFuncSetAttribute(kb_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_solve));
+        BCUDA(cudaFuncSetAttribute(kb_div_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kk::fft_smem_max()));
+        BCUDA(cudaFuncSetAttribute(kb_ifft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kk::fft_smem_max()));
+        BCUDA(cudaFuncSetAttribute(kb_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)kk::solve_smem_max()));
         BCUDA(cudaStreamSynchronize(stream));  // host tables go out of scope
         return KAMINO_OK;
     }
@@ -311,6 +312,7 @@ struct Engine {
                                : ((st == ST_DIV || st == ST_IFFT) ? shapes.fft_cta_per_sm
                                                                    : (st == ST_SOLVE ? shapes.solve_cta_per_sm
                                                                                      : shapes.adv_cta_per_sm));
+        if (st == ST_DIV || st == ST_IFFT) per = std::max(1, std::min(per, 2048 / fft_block));  // resident CTAs
         return std::max(1, std::min(n_items[st], per * nsm));
     }
 
@@ -322,11 +324,11 @@ struct Engine {
                                                                  n_items[ST_ADV], d_counters + ST_ADV, c, r, tpi);
         kb_geo<<<grid(ST_GEO), kk::ELEM_THREADS, 0, stream>>>(d_desc, d_items + item_off[ST_GEO], n_items[ST_GEO],
                                                                d_counters + ST_GEO, 1 - c, tpi);
-        kb_div_fft<<<grid(ST_DIV), 256, smem_fft, stream>>>(d_desc, d_items + item_off[ST_DIV], n_items[ST_DIV],
+        kb_div_fft<<<grid(ST_DIV), fft_block, smem_fft, stream>>>(d_desc, d_items + item_off[ST_DIV], n_items[ST_DIV],
                                                             d_counters + ST_DIV, 1 - c, c);
         kb_solve<<<grid(ST_SOLVE), kk::SOLVE_THREADS, smem_solve, stream>>>(
             d_desc, d_items + item_off[ST_SOLVE], n_items[ST_SOLVE], d_counters + ST_SOLVE);
-        kb_ifft<<<grid(ST_IFFT), 256, smem_fft, stream>>>(d_desc, d_items + item_off[ST_IFFT], n_items[ST_IFFT],
+        kb_ifft<<<grid(ST_IFFT), fft_block, smem_fft, stream>>>(d_desc, d_items + item_off[ST_IFFT], n_items[ST_IFFT],
                                                           d_counters + ST_IFFT, c, 1 - c);
         kb_vgrad<<<grid(ST_VGRAD), kk::ELEM_THREADS, 0, stream>>>(d_desc, d_items + item_off[ST_VGRAD],
                                                                    n_items[ST_VGRAD], d_counters + ST_VGRAD, c, 1 - c,
@@ -484,7 +486,7 @@ extern "C" int kamino_batch_time_steps(kamino_batch b, int n, int flush_l2, doub
     std::vector<cudaEvent_t> ev(2 * (size_t)n);
     for (auto& x : ev) BCUDA(cudaEventCreate(&x));
     for (int k = 0; k < n && !rc; k++) {
-        if (flush_l2) BCUDA(cudaMemsetAsync(b->flush, k & 0xff, b->flush_bytes, e.stream));
+        if (flush_l2) BCUDA(kk::flush_l2(b->flush, b->flush_bytes, k & 0xff, e.stream));
         BCUDA(cudaEventRecord(ev[2 * k], e.stream));
         rc = e.step_n(1);
         BCUDA(cudaEventRecord(ev[2 * k + 1], e.stream));

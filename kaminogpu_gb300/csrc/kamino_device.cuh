@@ -248,6 +248,98 @@ __device__ __forceinline__ float advect_cell(const float* __restrict__ u, const 
     return sample_cell<KIND>(field, i, j, -dp, -dtt, g, vf && KIND != KIND_CENTERED);
 }
 
+// sample_cell for positions whose rows it, it + 1 both lie in [0, pole_row):
+// plain bilinear, no pole branch, 32-bit indexing.  Anything else (a pole
+// row, a crossing, non-finite input) goes to sample_cell, so the result is
+// sample_cell's in every case.
+template <int KIND>
+__device__ __forceinline__ float sample_fast(const float* __restrict__ f, int i, int j, float x, float y,
+                                             const KGeo& g, bool vec_flip)
+{
+    const float kx = floorf(x), ky = floorf(y);
+    const int it = j + (int)ky;
+    const int pole_row = (KIND == KIND_VTHETA) ? g.nt - 2 : g.nt - 1;
+    if ((unsigned)it < (unsigned)pole_row) {
+        const float ax = x - kx, ay = y - ky;
+        const int ip = i + (int)kx;
+        const int i0 = ip & g.mask, i1 = (ip + 1) & g.mask;
+        const float* r0 = f + it * g.pitch;
+        const float* r1 = r0 + g.pitch;
+        const float v00 = __ldg(r0 + i0), v01 = __ldg(r0 + i1);
+        const float v10 = __ldg(r1 + i0), v11 = __ldg(r1 + i1);
+        return lerp2(lerp2(v00, v01, ax), lerp2(v10, v11, ax), ay);
+    }
+    return sample_cell<KIND>(f, i, j, x, y, g, vec_flip);
+}
+
+// RK2 step of one quantity from its start-point velocities (gu, gv):
+// advect_cell after its first two samples.
+template <int KIND>
+__device__ __forceinline__ float advect_from(const float* __restrict__ u, const float* __restrict__ v,
+                                             const float* __restrict__ field, int i, int j, float gu, float gv,
+                                             float cP, float cT, const KGeo& g, bool vf)
+{
+    constexpr float cgp = (KIND == KIND_VPHI) ? -0.5f : 0.0f;
+    constexpr float cgt = (KIND == KIND_VTHETA) ? 1.0f : 0.5f;
+    constexpr float ou_p = cgp + 0.5f, ou_t = cgt - 0.5f;
+    constexpr float ov_p = cgp, ov_t = cgt - 1.0f;
+    float dp = gu * cP, dtt = gv * cT;
+    float hp = 0.5f * dp, ht = 0.5f * dtt;
+    float mu = sample_fast<KIND_VPHI>(u, i, j, ou_p - hp, ou_t - ht, g, vf);
+    float mv = sample_fast<KIND_VTHETA>(v, i, j, ov_p - hp, ov_t - ht, g, vf);
+    dp = 0.5f * (mu + gu) * cP;
+    dtt = 0.5f * (mv + gv) * cT;
+    return sample_fast<KIND>(field, i, j, -dp, -dtt, g, vf && KIND != KIND_CENTERED);
+}
+
+// The three advected quantities of cell (i, j) in one thread: u_phi at
+// (i - 1/2, j + 1/2), u_theta at (i, j + 1) when j < nTheta - 1, thickness
+// at (i, j + 1/2).  In rows 1 .. nTheta-3 the start-point velocities are
+// fixed stencils of the grid (the samplers' alphas there are 0 or 1/2 and
+// no pole branch applies), shared between the three quantities:
+//   u_phi point:    u = u[j][i],        v = bilinear of v[j-1..j][i-1..i]
+//   u_theta point:  u = bilinear of u[j..j+1][i..i+1],  v = v[j][i]
+//   centred point:  u = mean of u[j][i..i+1],  v = mean of v[j-1..j][i]
+// The rows next to the poles run advect_cell for each quantity.
+__device__ __forceinline__ void advect_cell3(const float* __restrict__ u, const float* __restrict__ v,
+                                             const float* __restrict__ rho, int i, int j, float cPc, float cPv,
+                                             float cT, const KGeo& g, float& out_u, float& out_v, float& out_r)
+{
+    const bool vf = (g.flags & KAMINO_F_POLE_SIGN_FLIP) != 0;
+    if (j >= 1 && j <= g.nt - 3) {
+        const int im = (i - 1) & g.mask, ipl = (i + 1) & g.mask;
+        const float* uj = u + j * g.pitch;
+        const float* vj = v + j * g.pitch;
+        const float* vm = vj - g.pitch;
+        const float u00 = __ldg(uj + i), u01 = __ldg(uj + ipl);
+        const float u10 = __ldg(uj + g.pitch + i), u11 = __ldg(uj + g.pitch + ipl);
+        const float vmm = __ldg(vm + im), vm0 = __ldg(vm + i);
+        const float v0m = __ldg(vj + im), v00 = __ldg(vj + i);
+        const float gu_phi = u00;
+        const float gv_phi = lerp2(lerp2(vmm, vm0, 0.5f), lerp2(v0m, v00, 0.5f), 0.5f);
+        const float u_mid0 = lerp2(u00, u01, 0.5f);
+        const float gu_th = lerp2(u_mid0, lerp2(u10, u11, 0.5f), 0.5f);
+        const float gv_th = v00;
+        const float gu_c = u_mid0;
+        const float gv_c = lerp2(vm0, v00, 0.5f);
+        out_u = advect_from<KIND_VPHI>(u, v, u, i, j, gu_phi, gv_phi, cPc, cT, g, vf);
+        out_v = advect_from<KIND_VTHETA>(u, v, v, i, j, gu_th, gv_th, cPv, cT, g, vf);
+        out_r = advect_from<KIND_CENTERED>(u, v, rho, i, j, gu_c, gv_c, cPc, cT, g, vf);
+        return;
+    }
+    out_u = advect_cell<KIND_VPHI>(u, v, u, i, j, cPc, cT, g);
+    if (j < g.nt - 1) out_v = advect_cell<KIND_VTHETA>(u, v, v, i, j, cPv, cT, g);
+    out_r = advect_cell<KIND_CENTERED>(u, v, rho, i, j, cPc, cT, g);
+}
+
+// PTX rcp.approx.ftz.f32: the hardware reciprocal, within about an ulp.
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // ------------------------------------------------------------ geometric
 // The reference's solveCubic (KaminoCore.cu:421-454) with a = 0, in FP64,
 // used only when 1 + G v <= 0 (three real roots possible).
@@ -285,12 +377,12 @@ __device__ __forceinline__ float geo_root(float G, float uPrev, float vPrev)
     float a = __fmaf_rn(G, vPrev, 1.0f);
     if (a > 0.0f) {
         float G2 = G * G;
-        float x = uPrev / a;
+        float x = uPrev * rcp_approx(a);
         for (int k = 0; k < 40; k++) {
             float x2 = x * x;
             float f = __fmaf_rn(G2 * x2, x, __fmaf_rn(a, x, -uPrev));
             float df = __fmaf_rn(3.0f * G2, x2, a);
-            float dx = f / df;
+            float dx = f * rcp_approx(df);  // df >= a > 0
             x -= dx;
             if (!(fabsf(dx) > 5e-7f * fabsf(x))) break;
         }

@@ -141,6 +141,10 @@ extern "C" int kamino_projection_noalloc(int n_theta, const float* u_phi, const 
                            nt, NOALLOC_MAX_NT, NOALLOC_BYTES);
     if (!u_phi || !u_theta || !u_phi_out || !u_theta_out || !pressure_out)
         return kamino_fail(KAMINO_ERR_INVALID, "kamino_projection_noalloc: null field pointer");
+    for (const void* ptr : {(const void*)u_phi, (const void*)u_theta, (const void*)u_phi_out,
+                            (const void*)u_theta_out, (const void*)pressure_out})
+        if (reinterpret_cast<uintptr_t>(ptr) % 16 != 0)
+            return kamino_fail(KAMINO_ERR_INVALID, "kamino_projection_noalloc: field pointers must be 16-byte aligned");
     cudaStream_t stream = (cudaStream_t)stream_ptr;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -174,11 +178,10 @@ extern "C" int kamino_projection_noalloc(int n_theta, const float* u_phi, const 
     b.v[1] = u_theta_out;
     b.p = pressure_out;
     const int rpc = kk::fft_rows_per_cta(nt);
-    const int fft_threads = rpc * (nt / 4);
-    const size_t fft_smem = sizeof(float2) * 2 * (size_t)nt * rpc;
-    const int P = nt >= 256 ? nt / kk::SOLVE_THREADS : 1;
-    const size_t solve_smem = std::max(sizeof(kk::Row<float>) * (P == 1 ? nt : 2 * (nt / P)),
-                                       sizeof(double) * 2 * (size_t)(nt + 32));
+    const int fft_threads = kk::fft_threads(nt);
+    const size_t fft_smem = kk::fft_smem(nt);
+    const int P = kk::solve_rows(nt);
+    const size_t solve_smem = kk::solve_smem(nt);
     // same launches as kamino_projection (the divergence from face
     // velocities, the mode solves, the inverse FFT and both gradients)
     kk::k_div_fft<2><<<nt / rpc, fft_threads, fft_smem, stream>>>(g, b, 0, 1);
@@ -187,7 +190,7 @@ extern "C" int kamino_projection_noalloc(int n_theta, const float* u_phi, const 
     else
         kk::k_solve<2><<<nt, nt / 2, solve_smem, stream>>>(g, b, NOALLOC_FP64_MODES);
     kk::k_ifft_u<<<nt / rpc, fft_threads, fft_smem, stream>>>(g, b, 0, 1, 1);
-    const int nv = (nt - 1) * g.np;
+    const int nv = kk::elem_groups((nt - 1) * g.np);
     kk::k_vgrad<<<(nv + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS, kk::ELEM_THREADS, 0, stream>>>(g, b, 0, 1);
     e = cudaGetLastError();
     if (e != cudaSuccess)

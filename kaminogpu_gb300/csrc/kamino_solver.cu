@@ -187,7 +187,7 @@ void fp64_tables(int nt, int nmodes, const std::vector<double>& A, const std::ve
 {
     const size_t stride = kk::s64_stride(nt);
     out.assign(stride * (size_t)nmodes, 0.0);
-    const int P = nt >> 5;
+    const int TH = kk::s64_threads(nt), P = nt / TH;  // P >= 2
     struct R3 {
         double a, c, s;
     };
@@ -195,14 +195,13 @@ void fp64_tables(int nt, int nmodes, const std::vector<double>& A, const std::ve
         const double m2 = (double)(q + 1) * (q + 1);
         double* tb = out.data() + stride * q;
         double *dn = tb, *up = tb + nt, *bA = tb + 2 * nt, *bC = tb + 3 * nt, *bInv = tb + 4 * nt;
-        double *rF = tb + 5 * nt, *pl = rF + 32, *ph = pl + 6 * 64, *pinv = ph + 6 * 64;
+        double *rF = tb + 5 * nt, *pl = rF + kk::S64_TH, *ph = pl + kk::S64_L * kk::S64_R,
+               *pinv = ph + kk::S64_L * kk::S64_R;
         std::vector<R3> red;
-        if (P == 1) {
-            for (int i = 0; i < nt; i++) red.push_back({A[i], C[i], m2 * S[i]});
-        } else {
+        {
             std::vector<double> a(A), c(C), s(nt);
             for (int i = 0; i < nt; i++) s[i] = m2 * S[i];
-            for (int k = 0; k < 32; k++) {
+            for (int k = 0; k < TH; k++) {
                 const int f = k * P, l = f + P - 1;
                 for (int i = f + 2; i <= l; i++) {  // downward
                     double r = a[i] / (s[i - 1] + a[i - 1] + c[i - 1]);
@@ -245,8 +244,8 @@ void fp64_tables(int nt, int nmodes, const std::vector<double>& A, const std::ve
                 R3 lo = i - sft >= 0 ? red[i - sft] : R3{0, 0, 1};
                 R3 hi = i + sft < R ? red[i + sft] : R3{0, 0, 1};
                 double rl = red[i].a / (lo.s + lo.a + lo.c), rh = red[i].c / (hi.s + hi.a + hi.c);
-                pl[level * 64 + i] = rl;
-                ph[level * 64 + i] = rh;
+                pl[level * kk::S64_R + i] = rl;
+                ph[level * kk::S64_R + i] = rh;
                 nx[i] = {rl * lo.a, rh * hi.c, red[i].s + rl * lo.s + rh * hi.s};
             }
             red = nx;
@@ -254,9 +253,6 @@ void fp64_tables(int nt, int nmodes, const std::vector<double>& A, const std::ve
         for (int i = 0; i < R; i++) pinv[i] = 1.0 / (red[i].s + red[i].a + red[i].c);
     }
 }
-
-// FP32 rows per thread of k_solve and its block size.
-static int solve_rows(int nt) { return nt >= 256 ? nt / kk::SOLVE_THREADS : 1; }
 
 extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
 {
@@ -387,19 +383,13 @@ extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
         if (e != cudaSuccess) break;
         e = cudaStreamSynchronize(h->stream);  // host vectors above go out of scope
         if (e != cudaSuccess) break;
-        const int rpc = kk::fft_rows_per_cta(nt);
-        h->smem_div = sizeof(float2) * 2 * (size_t)nt * rpc;
+        h->smem_div = kk::fft_smem(nt);
         h->smem_ifft = h->smem_div;
-        const int P = solve_rows(nt);
-        const size_t red = sizeof(kk::Row<float>) * (P == 1 ? nt : 2 * (nt / P));
-        h->smem_solve = std::max(red, sizeof(double) * 2 * (size_t)(nt + 32));
-        e = cudaFuncSetAttribute(kk::k_div_fft<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem_div);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(kk::k_div_fft<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)h->smem_div);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(kk::k_ifft_u, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)h->smem_ifft);
+        h->smem_solve = kk::solve_smem(nt);
+        const int fmax = (int)kk::fft_smem_max();
+        e = cudaFuncSetAttribute(kk::k_div_fft<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, fmax);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(kk::k_div_fft<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, fmax);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(kk::k_ifft_u, cudaFuncAttributeMaxDynamicSharedMemorySize, fmax);
     } while (0);
     if (e != cudaSuccess) {
         rc = kamino_fail(KAMINO_ERR_CUDA, "kamino_create: %s", cudaGetErrorString(e));
@@ -411,28 +401,38 @@ extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
 }
 
 // ----------------------------------------------------------------- launches
+// Status of the launch just made (its returned status, else the last
+// error), naming the kernel on failure.
+static int launched(const char* name, cudaError_t ret = cudaSuccess)
+{
+    cudaError_t e = cudaGetLastError();
+    if (ret != cudaSuccess) e = ret;
+    return e == cudaSuccess ? KAMINO_OK : kamino_fail(KAMINO_ERR_CUDA, "%s launch: %s", name, cudaGetErrorString(e));
+}
+
 static int launch_advect(kamino_solver_s* h, int suv, int duv, int sr, int dr)
 {
     const KGeo& g = h->g;
     const int T = kk::ADV_THREADS;
-    int nb_u = (g.nt * g.np + T - 1) / T, nb_v = ((g.nt - 1) * g.np + T - 1) / T, nb_r = nb_u;
+    int nb_u, nb_v, nb_r;
+    kk::adv_tiles(g, nb_u, nb_v, nb_r);
     int nb_p = (int)((h->b.npart + T - 1) / T);
-    if (g.flags & KAMINO_F_REFERENCE_ROUNDING)
-        kk::k_advect<true><<<nb_u + nb_v + nb_r + nb_p, T, 0, h->stream>>>(g, h->b, suv, duv, sr, dr, nb_u, nb_v,
-                                                                           nb_r);
-    else
-        kk::k_advect<false><<<nb_u + nb_v + nb_r + nb_p, T, 0, h->stream>>>(g, h->b, suv, duv, sr, dr, nb_u, nb_v,
-                                                                            nb_r);
-    return cudaGetLastError() == cudaSuccess ? KAMINO_OK : KAMINO_ERR_CUDA;
+    const dim3 grid(nb_u + nb_v + nb_r + nb_p);
+    cudaError_t e = (g.flags & KAMINO_F_REFERENCE_ROUNDING)
+                        ? kk::launch_pdl(kk::k_advect<true>, grid, T, 0, h->stream, g, h->b, suv, duv, sr, dr, nb_u,
+                                         nb_v, nb_r)
+                        : kk::launch_pdl(kk::k_advect<false>, grid, T, 0, h->stream, g, h->b, suv, duv, sr, dr, nb_u,
+                                         nb_v, nb_r);
+    return launched("k_advect", e);
 }
 
 static int launch_geo(kamino_solver_s* h, int src)
 {
     const KGeo& g = h->g;
-    int n = g.nt * g.np;
-    kk::k_geo_centers<<<(n + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS, kk::ELEM_THREADS, 0, h->stream>>>(g, h->b,
-                                                                                                        src);
-    return cudaGetLastError() == cudaSuccess ? KAMINO_OK : KAMINO_ERR_CUDA;
+    int n = kk::elem_groups(g.nt * g.np);
+    cudaError_t e = kk::launch_pdl(kk::k_geo_centers, (n + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS,
+                                   kk::ELEM_THREADS, 0, h->stream, g, h->b, src);
+    return launched("k_geo_centers", e);
 }
 
 static int launch_assign(kamino_solver_s* h, int uv_out)
@@ -441,7 +441,7 @@ static int launch_assign(kamino_solver_s* h, int uv_out)
     int n = g.nt * g.np;
     kk::k_assign<<<(n + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS, kk::ELEM_THREADS, 0, h->stream>>>(g, h->b,
                                                                                                    uv_out);
-    return cudaGetLastError() == cudaSuccess ? KAMINO_OK : KAMINO_ERR_CUDA;
+    return launched("k_assign");
 }
 
 template <int MODE>
@@ -449,73 +449,79 @@ static int launch_div(kamino_solver_s* h, int uv_in, int uv_out)
 {
     const KGeo& g = h->g;
     const int rpc = kk::fft_rows_per_cta(g.nt);
-    kk::k_div_fft<MODE><<<g.nt / rpc, rpc * (g.nt / 4), h->smem_div, h->stream>>>(g, h->b, uv_in, uv_out);
-    return cudaGetLastError() == cudaSuccess ? KAMINO_OK : KAMINO_ERR_CUDA;
+    cudaError_t e = kk::launch_pdl(kk::k_div_fft<MODE>, g.nt / rpc, kk::fft_threads(g.nt), h->smem_div, h->stream, g,
+                                   h->b, uv_in, uv_out);
+    return launched("k_div_fft", e);
 }
 
 static int launch_solve(kamino_solver_s* h)
 {
     const KGeo& g = h->g;
-    const int P = solve_rows(g.nt), threads = g.nt / P;
+    const int P = kk::solve_rows(g.nt), threads = g.nt / P;
     const int grid = g.nt;  // blocks [0, nfp64) take the FP64 modes
+    void (*kern)(KGeo, KBufs, int) = nullptr;
     switch (P) {
-    case 1: kk::k_solve<1><<<grid, threads, h->smem_solve, h->stream>>>(g, h->b, h->nfp64); break;
-    case 2: kk::k_solve<2><<<grid, threads, h->smem_solve, h->stream>>>(g, h->b, h->nfp64); break;
-    case 4: kk::k_solve<4><<<grid, threads, h->smem_solve, h->stream>>>(g, h->b, h->nfp64); break;
-    case 8: kk::k_solve<8><<<grid, threads, h->smem_solve, h->stream>>>(g, h->b, h->nfp64); break;
-    case 16: kk::k_solve<16><<<grid, threads, h->smem_solve, h->stream>>>(g, h->b, h->nfp64); break;
-    default: return KAMINO_ERR_INVALID;
+    case 1: kern = kk::k_solve<1>; break;
+    case 2: kern = kk::k_solve<2>; break;
+    case 4: kern = kk::k_solve<4>; break;
+    case 8: kern = kk::k_solve<8>; break;
+    case 16: kern = kk::k_solve<16>; break;
+    default: return kamino_fail(KAMINO_ERR_INVALID, "no mode solve for %d rows per thread", P);
     }
-    return cudaGetLastError() == cudaSuccess ? KAMINO_OK : KAMINO_ERR_CUDA;
+    cudaError_t e = kk::launch_pdl(kern, grid, threads, h->smem_solve, h->stream, g, h->b, h->nfp64);
+    return launched("k_solve", e);
 }
 
 static int launch_ifft(kamino_solver_s* h, int uv_in, int uv_out)
 {
     const KGeo& g = h->g;
     const int rpc = kk::fft_rows_per_cta(g.nt);
-    kk::k_ifft_u<<<g.nt / rpc, rpc * (g.nt / 4), h->smem_ifft, h->stream>>>(g, h->b, uv_in, uv_out, 1);
-    if (cudaGetLastError() != cudaSuccess) return KAMINO_ERR_CUDA;
-    int n = (g.nt - 1) * g.np;
-    kk::k_vgrad<<<(n + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS, kk::ELEM_THREADS, 0, h->stream>>>(g, h->b, uv_in,
-                                                                                                  uv_out);
-    return cudaGetLastError() == cudaSuccess ? KAMINO_OK : KAMINO_ERR_CUDA;
+    cudaError_t e = kk::launch_pdl(kk::k_ifft_u, g.nt / rpc, kk::fft_threads(g.nt), h->smem_ifft, h->stream, g, h->b,
+                                   uv_in, uv_out, 1);
+    if (int rc = launched("k_ifft_u", e)) return rc;
+    int n = kk::elem_groups((g.nt - 1) * g.np);
+    e = kk::launch_pdl(kk::k_vgrad, (n + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS, kk::ELEM_THREADS, 0, h->stream, g,
+                       h->b, uv_in, uv_out);
+    return launched("k_vgrad", e);
 }
 
 // The fused step from parity (cu, cr); ev, when given, receives an external
 // event record before the first and after every kernel (kNumKernels + 1).
 static int enqueue_step(kamino_solver_s* h, int cu, int cr, cudaEvent_t* ev)
 {
-    int rc = 0;
+    cudaError_t pending = cudaGetLastError();
+    if (pending != cudaSuccess)
+        return kamino_fail(KAMINO_ERR_CUDA, "CUDA error pending before the step: %s", cudaGetErrorString(pending));
+    int rc = KAMINO_OK;
     auto mark = [&](int k) {
         if (ev) cudaEventRecordWithFlags(ev[k], h->stream, cudaEventRecordExternal);
     };
     mark(0);
-    rc |= launch_advect(h, cu, 1 - cu, cr, 1 - cr);
+    if (!rc) rc = launch_advect(h, cu, 1 - cu, cr, 1 - cr);
     mark(1);
-    rc |= launch_geo(h, 1 - cu);
+    if (!rc) rc = launch_geo(h, 1 - cu);
     mark(2);
-    rc |= launch_div<0>(h, 1 - cu, cu);
+    if (!rc) rc = launch_div<0>(h, 1 - cu, cu);
     mark(3);
-    rc |= launch_solve(h);
+    if (!rc) rc = launch_solve(h);
     mark(4);
-    {
+    if (!rc) {
         const KGeo& g = h->g;
         const int rpc = kk::fft_rows_per_cta(g.nt);
-        kk::k_ifft_u<<<g.nt / rpc, rpc * (g.nt / 4), h->smem_ifft, h->stream>>>(g, h->b, cu, 1 - cu, 1);
-        rc |= cudaGetLastError() == cudaSuccess ? 0 : KAMINO_ERR_CUDA;
+        cudaError_t e = kk::launch_pdl(kk::k_ifft_u, g.nt / rpc, kk::fft_threads(g.nt), h->smem_ifft, h->stream, g,
+                                       h->b, cu, 1 - cu, 1);
+        rc = launched("k_ifft_u", e);
     }
     mark(5);
-    {
+    if (!rc) {
         const KGeo& g = h->g;
-        int n = (g.nt - 1) * g.np;
-        kk::k_vgrad<<<(n + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS, kk::ELEM_THREADS, 0, h->stream>>>(g, h->b, cu,
-                                                                                                      1 - cu);
-        rc |= cudaGetLastError() == cudaSuccess ? 0 : KAMINO_ERR_CUDA;
+        int n = kk::elem_groups((g.nt - 1) * g.np);
+        cudaError_t e = kk::launch_pdl(kk::k_vgrad, (n + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS, kk::ELEM_THREADS,
+                                       0, h->stream, g, h->b, cu, 1 - cu);
+        rc = launched("k_vgrad", e);
     }
     mark(6);
-    return rc ? kamino_fail(KAMINO_ERR_CUDA, "kernel launch failed: %s",
-                            cudaGetErrorString(cudaGetLastError()))
-              : KAMINO_OK;
+    return rc;
 }
 
 static int get_graph(kamino_solver_s* h, int nsteps, cudaGraphExec_t* out)
@@ -614,7 +620,7 @@ extern "C" int kamino_advection(kamino_handle h)
     int rc = check_handle(h);
     if (rc) return rc;
     rc = launch_advect(h, h->cur_uv, 1 - h->cur_uv, h->cur_r, 1 - h->cur_r);
-    if (rc) return kamino_fail(rc, "k_advect launch: %s", cudaGetErrorString(cudaGetLastError()));
+    if (rc) return rc;
     h->cur_uv ^= 1;
     h->cur_r ^= 1;
     return KAMINO_OK;
@@ -626,7 +632,7 @@ extern "C" int kamino_geometric(kamino_handle h)
     if (rc) return rc;
     rc = launch_geo(h, h->cur_uv);
     if (!rc) rc = launch_assign(h, 1 - h->cur_uv);
-    if (rc) return kamino_fail(rc, "geometric launch: %s", cudaGetErrorString(cudaGetLastError()));
+    if (rc) return rc;
     h->cur_uv ^= 1;
     return KAMINO_OK;
 }
@@ -638,7 +644,7 @@ extern "C" int kamino_projection(kamino_handle h)
     rc = launch_div<2>(h, h->cur_uv, 1 - h->cur_uv);
     if (!rc) rc = launch_solve(h);
     if (!rc) rc = launch_ifft(h, h->cur_uv, 1 - h->cur_uv);
-    if (rc) return kamino_fail(rc, "projection launch: %s", cudaGetErrorString(cudaGetLastError()));
+    if (rc) return rc;
     h->cur_uv ^= 1;
     h->steps++;  // a full advection+geometric+projection sequence is a step
     h->time += h->g.dt;
@@ -864,7 +870,7 @@ extern "C" int kamino_time_steps(kamino_handle h, int n, int flush_l2, double* m
     std::vector<cudaEvent_t> ev(2 * (size_t)n, nullptr);
     for (auto& e : ev) KCUDA(cudaEventCreate(&e));
     for (int k = 0; k < n && rc == KAMINO_OK; k++) {
-        if (flush_l2) KCUDA(cudaMemsetAsync(h->flush, k & 0xff, h->flush_bytes, h->stream));
+        if (flush_l2) KCUDA(kk::flush_l2(h->flush, h->flush_bytes, k & 0xff, h->stream));
         KCUDA(cudaEventRecord(ev[2 * k], h->stream));
         rc = kamino_step(h, h->g.dt);
         KCUDA(cudaEventRecord(ev[2 * k + 1], h->stream));
@@ -915,7 +921,7 @@ extern "C" int kamino_time_kernels(kamino_handle h, int reps, int flush_l2, doub
                 break;
             }
         }
-        if (flush_l2) KCUDA(cudaMemsetAsync(h->flush, r & 0xff, h->flush_bytes, h->stream));
+        if (flush_l2) KCUDA(kk::flush_l2(h->flush, h->flush_bytes, r & 0xff, h->stream));
         KCUDA(cudaGraphLaunch(x, h->stream));
         KCUDA(cudaStreamSynchronize(h->stream));
         for (int k = 0; k < kNumKernels; k++) {

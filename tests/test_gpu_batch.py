@@ -111,3 +111,26 @@ def test_server_admission_respects_the_budget(kg):
             srv.poll()
     assert e.value.code == kg.ERR_BUDGET
     srv.close()
+
+
+def test_solvers_of_every_size_coexist(kg):
+    """Launch limits are process-wide per kernel: creating a sphere of one
+    size must not break stepping a sphere of another created before it."""
+    sizes = [32, 256, 64, 1024, 128, 512]
+    solvers = []
+    for k, nt in enumerate(sizes):
+        st = kg.make_initial_state(nt, lmax=4, seed=60 + k)
+        s = kg.KaminoSolver(config=kg.default_config(n_theta=nt, radius=1.0, dt=0.002))
+        s.load(st)
+        solvers.append(s)
+    for s in solvers:
+        s.step_n(2)
+    for k, (nt, s) in enumerate(zip(sizes, solvers)):
+        st = kg.make_initial_state(nt, lmax=4, seed=60 + k)
+        with kg.KaminoSolver(config=kg.default_config(n_theta=nt, radius=1.0, dt=0.002)) as ref:
+            ref.load(st)
+            ref.step_n(2)
+            a, b = s.fields(), ref.fields()
+        for key in ("u_phi", "u_theta", "thickness"):
+            assert np.array_equal(a[key].view(np.uint32), b[key].view(np.uint32)), (nt, key)
+        s.close()
