@@ -238,9 +238,8 @@ struct Engine {
                 return kamino_fail(KAMINO_ERR_INVALID, "batched spheres must share one buffer parity");
             }
             if (s.g.nt > 1024) return kamino_fail(KAMINO_ERR_INVALID, "batched spheres need n_theta <= 1024");
-            const int T = kk::ADV_THREADS;
             kk::adv_tiles(s.g, s.nb_u, s.nb_v, s.nb_r);
-            s.nb_adv = s.nb_u + s.nb_v + s.nb_r + (int)((s.b.npart + T - 1) / T);
+            s.nb_adv = s.nb_u + s.nb_v + s.nb_r + (int)((s.b.npart + kk::ADV_THREADS - 1) / kk::ADV_THREADS);
             s.nb_elem = (kk::elem_groups(s.g.nt * s.g.np) + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS;
             s.nb_fft = s.g.nt / kk::fft_rows_per_cta(s.g.nt);
             s.P = kk::solve_rows(s.g.nt);
@@ -312,7 +311,9 @@ struct Engine {
                                : ((st == ST_DIV || st == ST_IFFT) ? shapes.fft_cta_per_sm
                                                                    : (st == ST_SOLVE ? shapes.solve_cta_per_sm
                                                                                      : shapes.adv_cta_per_sm));
-        if (st == ST_DIV || st == ST_IFFT) per = std::max(1, std::min(per, 2048 / fft_block));  // resident CTAs
+        // no more CTAs than can be resident (threads, shared memory)
+        if (st == ST_DIV || st == ST_IFFT) per = std::max(1, std::min(per, 2048 / fft_block));
+
         return std::max(1, std::min(n_items[st], per * nsm));
     }
 

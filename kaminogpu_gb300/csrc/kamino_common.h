@@ -72,7 +72,7 @@ struct KBufs {
     float* cv;       // geometric scratch: v at cell centres
     float* p;        // pressure
     float2* spec;    // spectrum, [mode m-1][row], m = 1..nt
-    float2* sol;     // per-mode solution, [row][mode m-1]
+    float2* sol;     // per-mode solution, [mode m-1][row]
     double* s64;     // FP64 solve multipliers, s64_stride(nt) doubles per FP64 mode
     // per-row tables
     float* cof_c;    // dt / (R sinf((j+1/2)h))   (centred rows, u_phi rows)

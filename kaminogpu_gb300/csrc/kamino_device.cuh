@@ -248,25 +248,37 @@ __device__ __forceinline__ float advect_cell(const float* __restrict__ u, const 
     return sample_cell<KIND>(field, i, j, -dp, -dtt, g, vf && KIND != KIND_CENTERED);
 }
 
-// sample_cell for positions whose rows it, it + 1 both lie in [0, pole_row):
-// plain bilinear, no pole branch, 32-bit indexing.  Anything else (a pole
-// row, a crossing, non-finite input) goes to sample_cell, so the result is
-// sample_cell's in every case.
+// floor of x by a round-down add of 1.5 * 2^23 (exact for |x| < 2^22, which
+// every in-range cell offset is): returns floor(x) as an int and sets frac to
+// x - floor(x), the same value floorf gives.  Full-rate adds instead of a
+// rounding and a conversion; any other x (huge or non-finite) gives some int
+// that the callers' range checks send to the exact path.
+__device__ __forceinline__ int floor_frac(float x, float& frac)
+{
+    const float t = __fadd_rd(x, 12582912.0f);
+    frac = x - (t - 12582912.0f);
+    return __float_as_int(t) - 0x4B400000;
+}
+
+// sample_cell for positions whose rows it, it + 1 both lie in [0, pole_row)
+// and whose column pair does not straddle the phi seam: plain bilinear from
+// one address (the phi neighbour at +1, the next row at +pitch).  Anything
+// else (a pole row, a crossing, the seam, non-finite input) goes to
+// sample_cell, so the result is sample_cell's in every case.
 template <int KIND>
 __device__ __forceinline__ float sample_fast(const float* __restrict__ f, int i, int j, float x, float y,
                                              const KGeo& g, bool vec_flip)
 {
-    const float kx = floorf(x), ky = floorf(y);
-    const int it = j + (int)ky;
+    float ax, ay;
+    const int kx = floor_frac(x, ax), ky = floor_frac(y, ay);
+    const int it = j + ky;
+    const int i0 = (i + kx) & g.mask;
     const int pole_row = (KIND == KIND_VTHETA) ? g.nt - 2 : g.nt - 1;
-    if ((unsigned)it < (unsigned)pole_row) {
-        const float ax = x - kx, ay = y - ky;
-        const int ip = i + (int)kx;
-        const int i0 = ip & g.mask, i1 = (ip + 1) & g.mask;
-        const float* r0 = f + it * g.pitch;
-        const float* r1 = r0 + g.pitch;
-        const float v00 = __ldg(r0 + i0), v01 = __ldg(r0 + i1);
-        const float v10 = __ldg(r1 + i0), v11 = __ldg(r1 + i1);
+    if ((unsigned)it < (unsigned)pole_row && i0 != g.mask) {
+        const float* p0 = f + (it * g.pitch + i0);
+        const float* p1 = p0 + g.pitch;
+        const float v00 = __ldg(p0), v01 = __ldg(p0 + 1);
+        const float v10 = __ldg(p1), v11 = __ldg(p1 + 1);
         return lerp2(lerp2(v00, v01, ax), lerp2(v10, v11, ax), ay);
     }
     return sample_cell<KIND>(f, i, j, x, y, g, vec_flip);
@@ -300,21 +312,23 @@ __device__ __forceinline__ float advect_from(const float* __restrict__ u, const 
 //   u_phi point:    u = u[j][i],        v = bilinear of v[j-1..j][i-1..i]
 //   u_theta point:  u = bilinear of u[j..j+1][i..i+1],  v = v[j][i]
 //   centred point:  u = mean of u[j][i..i+1],  v = mean of v[j-1..j][i]
-// The rows next to the poles run advect_cell for each quantity.
+// The rows next to the poles and the two columns at the phi seam run
+// advect_cell for each quantity.
 __device__ __forceinline__ void advect_cell3(const float* __restrict__ u, const float* __restrict__ v,
                                              const float* __restrict__ rho, int i, int j, float cPc, float cPv,
                                              float cT, const KGeo& g, float& out_u, float& out_v, float& out_r)
 {
     const bool vf = (g.flags & KAMINO_F_POLE_SIGN_FLIP) != 0;
-    if (j >= 1 && j <= g.nt - 3) {
-        const int im = (i - 1) & g.mask, ipl = (i + 1) & g.mask;
-        const float* uj = u + j * g.pitch;
-        const float* vj = v + j * g.pitch;
+    if (j >= 1 && j <= g.nt - 3 && i >= 1 && i < g.mask) {
+        // columns i - 1 .. i + 1 without wrapping: neighbours at +-1
+        const float* uj = u + (j * g.pitch + i);
+        const float* ujn = uj + g.pitch;
+        const float* vj = v + (j * g.pitch + i);
         const float* vm = vj - g.pitch;
-        const float u00 = __ldg(uj + i), u01 = __ldg(uj + ipl);
-        const float u10 = __ldg(uj + g.pitch + i), u11 = __ldg(uj + g.pitch + ipl);
-        const float vmm = __ldg(vm + im), vm0 = __ldg(vm + i);
-        const float v0m = __ldg(vj + im), v00 = __ldg(vj + i);
+        const float u00 = __ldg(uj), u01 = __ldg(uj + 1);
+        const float u10 = __ldg(ujn), u11 = __ldg(ujn + 1);
+        const float vmm = __ldg(vm - 1), vm0 = __ldg(vm);
+        const float v0m = __ldg(vj - 1), v00 = __ldg(vj);
         const float gu_phi = u00;
         const float gv_phi = lerp2(lerp2(vmm, vm0, 0.5f), lerp2(v0m, v00, 0.5f), 0.5f);
         const float u_mid0 = lerp2(u00, u01, 0.5f);
@@ -364,6 +378,15 @@ __device__ __forceinline__ double ref_solve_cubic64(double b, double c)
     return A + B;
 }
 
+// The FP64 branch of geo_root (1 + G v <= 0).  Not inlined, so none of its
+// double arithmetic is evaluated ahead of the branch for every cell (FP64 is
+// 1/64 of the FP32 rate on GB300).
+static __device__ __noinline__ float geo_root_fp64(float G, float uPrev, float vPrev)
+{
+    double G2 = (double)G * (double)G;
+    return (float)ref_solve_cubic64(((double)G * vPrev + 1.0) / G2, -(double)uPrev / G2);
+}
+
 // u' of geometricFillKernel (KaminoCore.cu:494-508): the root the reference
 // takes of u^3 + ((G v + 1)/G^2) u - uPrev/G^2 = 0.  When 1 + G v > 0 that
 // root is unique and g(u) = G^2 u^3 + (1 + G v) u - uPrev is increasing and
@@ -388,8 +411,7 @@ __device__ __forceinline__ float geo_root(float G, float uPrev, float vPrev)
         }
         return x;
     }
-    double G2 = (double)G * (double)G;
-    return (float)ref_solve_cubic64(((double)G * vPrev + 1.0) / G2, -(double)uPrev / G2);
+    return geo_root_fp64(G, uPrev, vPrev);
 }
 
 // ---------------------------------------------------------------- FFT

@@ -113,10 +113,11 @@ __device__ __forceinline__ void advect_particle(const KGeo& g, const float* __re
     out = make_float2(updatedPhi, updatedTheta);
 }
 
-// Advection tiles of one sphere (adv_tiles): the cell-exact kernel takes one
-// cell per thread and advects its three quantities (nb_u tiles, nb_v = nb_r
-// = 0); the reference-rounding kernel takes one point per thread, nb_u tiles
-// of u_phi, nb_v of u_theta, nb_r of thickness.  Particle tiles follow.
+// Advection tiles of one sphere: the cell-exact kernel takes one cell per
+// thread and advects its three quantities (nb_u tiles, nb_v = nb_r = 0); the
+// reference-rounding kernel takes one point per thread, nb_u tiles of u_phi,
+// nb_v of u_theta, nb_r of thickness.  Particle tiles follow; every tile is
+// ADV_THREADS threads.
 inline void adv_tiles(const KGeo& g, int& nb_u, int& nb_v, int& nb_r)
 {
     const int T = ADV_THREADS;
@@ -772,17 +773,47 @@ __host__ __device__ inline size_t s64_smem(int nt)
     const int th = s64_threads(nt);
     return sizeof(float2) * (size_t)(nt + th) + sizeof(double2) * 2 * (size_t)th;
 }
+// the same with the mode's multiplier table staged in front (k_solve64)
+__host__ __device__ inline size_t s64_smem_staged(int nt) { return sizeof(double) * s64_stride(nt) + s64_smem(nt); }
+inline size_t s64_smem_staged_max()
+{
+    size_t m = 0;
+    for (int nt = 32; nt <= 2048; nt *= 2) m = s64_smem_staged(nt) > m ? s64_smem_staged(nt) : m;
+    return m;
+}
+
+// bytes (a multiple of 16, both addresses 16-byte aligned) copied global ->
+// shared by the CTA with 16-byte cp.async, all issued before the wait, which
+// waits for this thread's own copies; the caller synchronises the CTA.
+__device__ __forceinline__ void copy_async_g2s(void* dst, const void* src, size_t bytes, int t)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    const char* sp = static_cast<const char*>(src);
+    for (size_t o = (size_t)t * 16; o < bytes; o += (size_t)blockDim.x * 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d + (unsigned)o), "l"(sp + o) : "memory");
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
 
 // FP64 solve of mode m: every thread of the CTA calls it (it synchronises);
-// threads t >= nTheta/P own no rows.
-template <int P>
+// threads t >= nTheta/P own no rows.  STAGED: the mode's multiplier table is
+// first copied into shared memory (s64_smem_staged bytes), so the
+// reduction's per-level multipliers are shared-memory reads rather than a
+// global round trip per level.
+template <int P, bool STAGED>
 __device__ void solve_mode64(const KGeo& g, const KBufs& b, int m, unsigned char* smraw, int t)
 {
     const int n = g.nt, TH = n / P, R = 2 * TH;
     const bool active = t < TH;
     const double* tb = b.s64 + (size_t)(m - 1) * s64_stride(n);
+    if (STAGED) {
+        double* st = reinterpret_cast<double*>(smraw);
+        copy_async_g2s(st, tb, sizeof(double) * s64_stride(n), t);
+        tb = st;
+        smraw += sizeof(double) * s64_stride(n);
+    }
     const double *dn = tb, *up = tb + n, *bA = tb + 2 * n, *bC = tb + 3 * n, *bInv = tb + 4 * n;
     const double *rF = tb + 5 * n, *pl = rF + S64_TH, *ph = pl + S64_L * S64_R, *pinv = ph + S64_L * S64_R;
+    auto ld = [](const double* p) { return STAGED ? *p : __ldg(p); };
     const float2* __restrict__ col = b.spec + (size_t)(m - 1) * n;
     float2* __restrict__ sol = b.sol + (size_t)(m - 1) * n;
     float2* cs = reinterpret_cast<float2*>(smraw);             // n + TH slots
@@ -801,7 +832,7 @@ __device__ void solve_mode64(const KGeo& g, const KBufs& b, int m, unsigned char
         }
 #pragma unroll
         for (int q = 2; q < P; q++) {
-            const double r = __ldg(dn + f + q);
+            const double r = ld(dn + f + q);
             Dr[q] = fma(r, Dr[q - 1], Dr[q]);
             Di[q] = fma(r, Di[q - 1], Di[q]);
         }
@@ -809,14 +840,14 @@ __device__ void solve_mode64(const KGeo& g, const KBufs& b, int m, unsigned char
         Li = Di[P - 1];
 #pragma unroll
         for (int q = P - 3; q >= 1; q--) {
-            const double r = __ldg(up + f + q);
+            const double r = ld(up + f + q);
             Dr[q] = fma(r, Dr[q + 1], Dr[q]);
             Di[q] = fma(r, Di[q + 1], Di[q]);
         }
         Fr = Dr[0];
         Fi = Di[0];
         if (P >= 3) {
-            const double r = __ldg(rF + t);
+            const double r = ld(rF + t);
             Fr = fma(r, Dr[1], Fr);
             Fi = fma(r, Di[1], Fi);
         }
@@ -836,7 +867,7 @@ __device__ void solve_mode64(const KGeo& g, const KBufs& b, int m, unsigned char
             const double2 z = make_double2(0.0, 0.0);
             const double2 lf = iF - s >= 0 ? xs[iF - s] : z, hf = iF + s < R ? xs[iF + s] : z;
             const double2 ll = iL - s >= 0 ? xs[iL - s] : z, hl = iL + s < R ? xs[iL + s] : z;
-            const double aF = __ldg(L0 + iF), cF = __ldg(H0 + iF), aL = __ldg(L0 + iL), cL = __ldg(H0 + iL);
+            const double aF = ld(L0 + iF), cF = ld(H0 + iF), aL = ld(L0 + iL), cL = ld(H0 + iL);
             Fr = fma(aF, lf.x, fma(cF, hf.x, Fr));
             Fi = fma(aF, lf.y, fma(cF, hf.y, Fi));
             Lr = fma(aL, ll.x, fma(cL, hl.x, Lr));
@@ -845,13 +876,13 @@ __device__ void solve_mode64(const KGeo& g, const KBufs& b, int m, unsigned char
         __syncthreads();
     }
     if (active) {
-        const double pF = __ldg(pinv + iF), pL = __ldg(pinv + iL);
+        const double pF = ld(pinv + iF), pL = ld(pinv + iL);
         const double xfr = Fr * pF, xfi = Fi * pF, xlr = Lr * pL, xli = Li * pL;
         cs[f + t] = make_float2((float)xfr, (float)xfi);
         cs[f + P - 1 + t] = make_float2((float)xlr, (float)xli);
 #pragma unroll
         for (int q = 1; q < P - 1; q++) {
-            const double a = __ldg(bA + f + q), c = __ldg(bC + f + q), iv = __ldg(bInv + f + q);
+            const double a = ld(bA + f + q), c = ld(bC + f + q), iv = ld(bInv + f + q);
             const double xr = fma(a, xfr, fma(c, xlr, Dr[q])) * iv;
             const double xi = fma(a, xfi, fma(c, xli, Di[q])) * iv;
             cs[f + q + t] = make_float2((float)xr, (float)xi);
@@ -864,10 +895,10 @@ __device__ void solve_mode64(const KGeo& g, const KBufs& b, int m, unsigned char
 __device__ __forceinline__ void solve_mode64_any(const KGeo& g, const KBufs& b, int m, unsigned char* sm, int t)
 {
     switch (g.nt / s64_threads(g.nt)) {
-    case 2: solve_mode64<2>(g, b, m, sm, t); break;
-    case 4: solve_mode64<4>(g, b, m, sm, t); break;
-    case 8: solve_mode64<8>(g, b, m, sm, t); break;
-    default: solve_mode64<16>(g, b, m, sm, t); break;
+    case 2: solve_mode64<2, false>(g, b, m, sm, t); break;
+    case 4: solve_mode64<4, false>(g, b, m, sm, t); break;
+    case 8: solve_mode64<8, false>(g, b, m, sm, t); break;
+    default: solve_mode64<16, false>(g, b, m, sm, t); break;
     }
 }
 
@@ -927,10 +958,30 @@ __global__ void __launch_bounds__(SOLVE_THREADS) k_solve(KGeo g, KBufs b, int nf
     if ((int)blockIdx.x < nfp64) {
         // FP64 rows per thread: nt / s64_threads(nt), which is P for nt >= 256
         // and 2 below
-        solve_mode64<(P < 2 ? 2 : P)>(g, b, blockIdx.x + 1, smraw, threadIdx.x);
+        solve_mode64<(P < 2 ? 2 : P), false>(g, b, blockIdx.x + 1, smraw, threadIdx.x);
         return;
     }
     solve_mode32<P>(g, b, (int)blockIdx.x + 1, smraw, threadIdx.x);
+}
+
+// The step's mode solves as two kernels on parallel branches of the step
+// graph: k_solve64 takes modes 1 .. nfp64 (one CTA each, nt / P64 threads),
+// k_solve32 modes nfp64 + 1 .. nt, so the FP32 kernel carries neither the
+// FP64 code's registers nor its longer CTAs.
+template <int P>
+__global__ void __launch_bounds__(SOLVE_THREADS, 8) k_solve32(KGeo g, KBufs b, int nfp64)
+{
+    pdl_wait();
+    extern __shared__ __align__(16) unsigned char smraw[];
+    solve_mode32<P>(g, b, (int)blockIdx.x + nfp64 + 1, smraw, threadIdx.x);
+}
+
+template <int P64>
+__global__ void __launch_bounds__(S64_TH) k_solve64(KGeo g, KBufs b)
+{
+    pdl_wait();
+    extern __shared__ __align__(16) unsigned char smraw[];
+    solve_mode64<P64, true>(g, b, (int)blockIdx.x + 1, smraw, threadIdx.x);
 }
 
 // ---------------------------------------------------- inverse FFT + u update

@@ -5,7 +5,9 @@
 // 749-842).  All state lives in one device arena allocated at create time;
 // a step is five kernel launches (kamino_kernels.cuh) replayed from a CUDA
 // graph on the handle's own stream.  Every failure returns a status code.
+#include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -45,6 +47,8 @@ struct kamino_solver_s {
     KBufs b;
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;  // FP64 mode solves, a parallel branch of the step
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     void* arena = nullptr;
     size_t arena_bytes = 0;
     int cur_uv = 0, cur_r = 0;  // which buffer holds (u, v) and (thickness, particles)
@@ -143,6 +147,9 @@ extern "C" int kamino_destroy(kamino_handle h)
     if (h->arena) cudaFree(h->arena);
     if (h->flush) cudaFree(h->flush);
     if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->side) cudaStreamDestroy(h->side);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
     cudaSetDevice(dev0);
     delete h;
     return KAMINO_OK;
@@ -286,6 +293,9 @@ extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
     const size_t s64 = align_up(sizeof(double) * kk::s64_stride(nt) * std::max(h->nfp64, 1));
     size_t total = 9 * field + 2 * spec + 2 * part + 13 * rowf + 4 * rowd + tw + rt + s64;
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&h->arena, total);
     if (e != cudaSuccess) {
         int code = e == cudaErrorMemoryAllocation ? KAMINO_ERR_ALLOC : KAMINO_ERR_CUDA;
@@ -386,6 +396,12 @@ extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
         h->smem_div = kk::fft_smem(nt);
         h->smem_ifft = h->smem_div;
         h->smem_solve = kk::solve_smem(nt);
+        const int smax = (int)kk::s64_smem_staged_max();
+        e = cudaFuncSetAttribute(kk::k_solve64<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(kk::k_solve64<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(kk::k_solve64<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(kk::k_solve64<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+        if (e != cudaSuccess) break;
         const int fmax = (int)kk::fft_smem_max();
         e = cudaFuncSetAttribute(kk::k_div_fft<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, fmax);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(kk::k_div_fft<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, fmax);
@@ -459,17 +475,30 @@ static int launch_solve(kamino_solver_s* h)
     const KGeo& g = h->g;
     const int P = kk::solve_rows(g.nt), threads = g.nt / P;
     const int grid = g.nt;  // blocks [0, nfp64) take the FP64 modes
-    void (*kern)(KGeo, KBufs, int) = nullptr;
-    switch (P) {
-    case 1: kern = kk::k_solve<1>; break;
-    case 2: kern = kk::k_solve<2>; break;
-    case 4: kern = kk::k_solve<4>; break;
-    case 8: kern = kk::k_solve<8>; break;
-    case 16: kern = kk::k_solve<16>; break;
+    (void)grid;
+    void (*k32)(KGeo, KBufs, int) = nullptr;
+    void (*k64)(KGeo, KBufs) = nullptr;
+    switch (P) {  // FP64 rows per thread: P for nt >= 256, 2 below
+    case 1: k32 = kk::k_solve32<1>, k64 = kk::k_solve64<2>; break;
+    case 2: k32 = kk::k_solve32<2>, k64 = kk::k_solve64<2>; break;
+    case 4: k32 = kk::k_solve32<4>, k64 = kk::k_solve64<4>; break;
+    case 8: k32 = kk::k_solve32<8>, k64 = kk::k_solve64<8>; break;
+    case 16: k32 = kk::k_solve32<16>, k64 = kk::k_solve64<16>; break;
     default: return kamino_fail(KAMINO_ERR_INVALID, "no mode solve for %d rows per thread", P);
     }
-    cudaError_t e = kk::launch_pdl(kern, grid, threads, h->smem_solve, h->stream, g, h->b, h->nfp64);
-    return launched("k_solve", e);
+    if (h->nfp64 > 0) {  // fork the FP64 modes onto the side stream
+        KCUDA(cudaEventRecord(h->ev_fork, h->stream));
+        KCUDA(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
+        k64<<<h->nfp64, kk::s64_threads(g.nt), kk::s64_smem_staged(g.nt), h->side>>>(g, h->b);
+        if (int rc = launched("k_solve64")) return rc;
+        KCUDA(cudaEventRecord(h->ev_join, h->side));
+    }
+    if (g.nt > h->nfp64) {
+        cudaError_t e = kk::launch_pdl(k32, g.nt - h->nfp64, threads, h->smem_solve, h->stream, g, h->b, h->nfp64);
+        if (int rc = launched("k_solve32", e)) return rc;
+    }
+    if (h->nfp64 > 0) KCUDA(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
+    return KAMINO_OK;
 }
 
 static int launch_ifft(kamino_solver_s* h, int uv_in, int uv_out)
@@ -763,7 +792,8 @@ extern "C" int kamino_time_elapsed(kamino_handle h, double* t, int64_t* steps)
     return KAMINO_OK;
 }
 
-extern "C" int kamino_launches_per_step(kamino_handle) { return kNumKernels; }
+// six kernels, plus k_solve64 on the FP64 branch when modes run in FP64
+extern "C" int kamino_launches_per_step(kamino_handle h) { return kNumKernels + (h && h->nfp64 > 0 ? 1 : 0); }
 
 extern "C" int kamino_device_bytes(kamino_handle h, size_t* bytes)
 {
@@ -797,6 +827,18 @@ static float* field_dev(kamino_solver_s* h, int field)
     return nullptr;
 }
 
+// bytes between device memory d and host memory hp.  (Measured on GB300: the
+// copy engines reach the host link's rate; an SM copy kernel over the link is
+// no faster.)
+static int copy_host(kamino_solver_s* h, float* d, void* hp, size_t bytes, bool to_device)
+{
+    if (to_device)
+        KCUDA(cudaMemcpyAsync(d, hp, bytes, cudaMemcpyHostToDevice, h->stream));
+    else
+        KCUDA(cudaMemcpyAsync(hp, d, bytes, cudaMemcpyDeviceToHost, h->stream));
+    return KAMINO_OK;
+}
+
 static int copy_field(kamino_solver_s* h, int field, void* other, size_t pitch, bool to_device,
                       cudaMemcpyKind kind, bool sync)
 {
@@ -810,15 +852,25 @@ static int copy_field(kamino_solver_s* h, int field, void* other, size_t pitch, 
     if (field == KAMINO_PARTICLES) {
         size_t n = sizeof(float2) * (size_t)h->b.npart;
         if (n == 0) return KAMINO_OK;
-        if (to_device)
+        if (kind != cudaMemcpyDeviceToDevice) {
+            if ((rc = copy_host(h, d, other, n, to_device))) return rc;
+        } else if (to_device) {
             KCUDA(cudaMemcpyAsync(d, other, n, kind, h->stream));
-        else
+        } else {
             KCUDA(cudaMemcpyAsync(other, d, n, kind, h->stream));
+        }
     } else {
         const size_t w = sizeof(float) * h->g.np;
         if (pitch == 0) pitch = w;
         if (pitch < w) return kamino_fail(KAMINO_ERR_INVALID, "pitch %zu < row bytes %zu", pitch, w);
-        if (to_device)
+        if (pitch == w && kind != cudaMemcpyDeviceToDevice) {  // dense rows on both sides: one linear copy
+            if ((rc = copy_host(h, d, other, w * rows, to_device))) return rc;
+        } else if (pitch == w) {
+            if (to_device)
+                KCUDA(cudaMemcpyAsync(d, other, w * rows, kind, h->stream));
+            else
+                KCUDA(cudaMemcpyAsync(other, d, w * rows, kind, h->stream));
+        } else if (to_device)
             KCUDA(cudaMemcpy2DAsync(d, w, other, pitch, w, rows, kind, h->stream));
         else
             KCUDA(cudaMemcpy2DAsync(other, pitch, d, w, w, rows, kind, h->stream));
