@@ -7,9 +7,9 @@ modes |m| <= 4 solved in FP64.  A "step" is one stepForward of that sphere.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-value: device time of K steps (CUDA events on the solver's stream, a 256 MiB
-  buffer written between steps so each step starts with a cold L2; the state
-  is 25 MB and would otherwise sit in the 129 MB L2).
+value: device time of K steps (CUDA events on the solver's stream; a 256 MiB
+  buffer written and then read between steps, so each step starts from a cold
+  and clean L2; the state is 25 MB and would otherwise sit in the 129 MB L2).
 e2e:   the same steps through the public C ABI with host buffers: every step
   copies u_phi, u_theta, thickness in from pinned host memory, steps, and
   copies them back.
@@ -232,7 +232,7 @@ def run_ours(args, ws, rank, local, dist):
         "data": "synthetic: seeded l<=32 spherical-harmonic stream function + Gaussian vortex (sigma 0.1 rad), "
                 "max|u|=1; thickness 1+0.05U(-1,1)",
         "config": {"workload": "plain solver, one sphere nTheta=1024 nPhi=2048, radius 1, dt=0.001 (precision form)",
-                   "sampler": "cell-exact", "fp64_modes": 4, "l2": "256 MiB buffer written before every timed step",
+                   "sampler": "cell-exact", "fp64_modes": 4, "l2": "256 MiB buffer written then read before every timed step (cold, clean L2)",
                    "parallelism": "replicas" if ws > 1 else "single GPU", "wall_s_timed_region": wall},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": sum(nbytes.values()),
                 "d2h_bytes_per_step": sum(nbytes.values())},

@@ -267,7 +267,7 @@ struct Engine {
                 case ST_VGRAD: count = (s.nb_elem + tpi - 1) / tpi; break;
                 case ST_DIV:
                 case ST_IFFT: count = s.nb_fft; break;
-                case ST_SOLVE: count = s.g.nt; break;
+                case ST_SOLVE: count = s.g.nt + s.nfp64; break;  // two tiles per FP64 mode
                 }
                 for (int t = 0; t < count; t++) items.push_back(make_int2(i, t));
             }

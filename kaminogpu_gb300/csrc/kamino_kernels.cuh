@@ -282,9 +282,10 @@ __device__ __forceinline__ void dft4(float2& a, float2& b, float2& c, float2& d)
 // which consecutive lanes walk the R rows of one Fourier mode (the
 // spectrum/solution transposes, whose global accesses then fill whole 32-byte
 // sectors).
-__host__ __device__ inline int fft_rows_per_cta(int nt) { return nt >= 2048 ? 2 : (nt >= 256 ? 4 : 1024 / nt); }
-__host__ __device__ inline int fft_threads(int nt) { return fft_rows_per_cta(nt) * (nt >> 2); }
-__host__ __device__ inline int fft_stride(int nt) { return nt + ((nt == 32 || nt >= 2048) ? 8 : 4); }
+__host__ __device__ constexpr int fft_rows_per_cta(int nt) { return nt >= 2048 ? 2 : (nt >= 256 ? 4 : 1024 / nt); }
+__host__ __device__ constexpr int fft_threads(int nt) { return fft_rows_per_cta(nt) * (nt >> 2); }
+__host__ __device__ constexpr int fft_stride(int nt) { return nt + ((nt == 32 || nt >= 2048) ? 8 : 4); }
+__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n >> 1); }
 __host__ __device__ inline size_t fft_smem(int nt)
 {
     return sizeof(float2) * 2 * (size_t)fft_rows_per_cta(nt) * fft_stride(nt);
@@ -293,55 +294,40 @@ __device__ __forceinline__ int fsw(int a) { return a ^ ((a >> 2) & 15); }
 
 // Complex FFT of length N (power of two, >= 32) by T = N/4 threads per row,
 // Stockham autosort: radix-4 stages, then one radix-2 stage when log2 N is
-// odd.  Thread t enters holding x[t + r T], r = 0..3.  Every thread of the
-// CTA calls it (it synchronises); inactive threads only synchronise.  The
+// odd (N is a template parameter: the stages unroll with constant strides).
+// Thread t enters holding x[t + r T], r = 0..3.  Every thread of the CTA
+// calls it (it synchronises); inactive threads only synchronise.  The
 // transform ends in natural order (swizzled slots) in rowA or rowB; returns
 // true for rowB.  tw[k] = e^{-2 pi i k/N}.
-template <bool INV>
-__device__ __forceinline__ bool stockham(float2 v[4], float2* rowA, float2* rowB, int N, int t,
+template <bool INV, int N>
+__device__ __forceinline__ bool stockham(float2 v[4], float2* rowA, float2* rowB, int t,
                                          const float2* __restrict__ tw, bool active)
 {
-    const int T = N >> 2;
+    constexpr int T = N >> 2, LOG2N = ilog2c(N), NR4 = LOG2N / 2;
+    constexpr bool R2 = (LOG2N & 1) != 0;
     float2* out = rowA;
     bool inB = false;
-    int Ns = 1, ls = 0;
-    while (true) {
-        if (4 * Ns <= N) {
-            if (active) {
-                const int k = t & (Ns - 1);
-                if (Ns > 1) {
-                    const int step = N >> (ls + 2);
 #pragma unroll
-                    for (int r = 1; r < 4; r++) {
-                        float2 w = __ldg(tw + r * k * step);
-                        if (INV) w.y = -w.y;
-                        v[r] = cmul(w, v[r]);
-                    }
-                }
-                dft4<INV>(v[0], v[1], v[2], v[3]);
-                const int base = ((t - k) << 2) + k;
+    for (int st = 0; st < NR4; st++) {
+        const int Ns = 1 << (2 * st);
+        if (active) {
+            const int k = t & (Ns - 1);
+            if (st > 0) {
+                const int step = N >> (2 * st + 2);
 #pragma unroll
-                for (int r = 0; r < 4; r++) out[fsw(base + r * Ns)] = v[r];
-            }
-            Ns <<= 2;
-            ls += 2;
-        } else {  // radix-2, Ns = N/2: butterflies t and t + T
-            if (active) {
-#pragma unroll
-                for (int q = 0; q < 2; q++) {
-                    const int idx = t + q * T;
-                    float2 w = __ldg(tw + idx);
+                for (int r = 1; r < 4; r++) {
+                    float2 w = __ldg(tw + r * k * step);
                     if (INV) w.y = -w.y;
-                    float2 y = cmul(w, v[q + 2]);
-                    out[fsw(idx)] = f2add(v[q], y);
-                    out[fsw(idx + Ns)] = f2sub(v[q], y);
+                    v[r] = cmul(w, v[r]);
                 }
             }
-            Ns <<= 1;
-            ls += 1;
+            dft4<INV>(v[0], v[1], v[2], v[3]);
+            const int base = ((t - k) << 2) + k;
+#pragma unroll
+            for (int r = 0; r < 4; r++) out[fsw(base + r * Ns)] = v[r];
         }
         __syncthreads();
-        if (Ns >= N) return inB;
+        if (st == NR4 - 1 && !R2) return inB;
         if (active) {
 #pragma unroll
             for (int r = 0; r < 4; r++) v[r] = out[fsw(t + r * T)];
@@ -349,6 +335,22 @@ __device__ __forceinline__ bool stockham(float2 v[4], float2* rowA, float2* rowB
         out = inB ? rowA : rowB;
         inB = !inB;
     }
+    if (R2) {  // radix-2, Ns = N/2: butterflies t and t + T
+        constexpr int Ns = N / 2;
+        if (active) {
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const int idx = t + q * T;
+                float2 w = __ldg(tw + idx);
+                if (INV) w.y = -w.y;
+                float2 y = cmul(w, v[q + 2]);
+                out[fsw(idx)] = f2add(v[q], y);
+                out[fsw(idx + Ns)] = f2sub(v[q], y);
+            }
+        }
+        __syncthreads();
+    }
+    return inB;
 }
 
 // Divergence and forward real FFT of latitude rows.
@@ -358,16 +360,17 @@ __device__ __forceinline__ bool stockham(float2 v[4], float2* rowA, float2* rowB
 // spec[(m-1)*nt + row].  c_0 (the dropped m = 0 mode) is never formed.
 // Tile `blk` = rows [blk*R, blk*R + R); every thread of the CTA calls it,
 // threads past R*N/4 only synchronise and help with the spectrum stores.
-template <int MODE>
-__device__ __forceinline__ void div_fft_tile(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int blk,
-                                             int tid, float2* sm2)
+template <int MODE, int N>
+__device__ __forceinline__ void div_fft_tile_n(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int blk,
+                                               int tid, float2* sm2)
 {
-    const int N = g.nt, T = N >> 2, R = fft_rows_per_cta(N), S = fft_stride(N);
-    const int lgT = g.log2nt - 2, lgR = 31 - __clz(R);
+    constexpr int T = N >> 2, R = fft_rows_per_cta(N), S = fft_stride(N);
+    constexpr int lgT = ilog2c(T), lgR = ilog2c(R);
     const int lr = tid >> lgT, t = tid & (T - 1);
     const bool active = lr < R;
     const int j = blk * R + lr;
-    const int np = g.np, mask = g.mask, lane = tid & 31;
+    constexpr int np = 2 * N, mask = 2 * N - 1;
+    const int lane = tid & 31;
     const float* __restrict__ cu = b.cu;
     const float* __restrict__ cv = b.cv;
     const float* __restrict__ uf = b.u[uv_in];
@@ -454,13 +457,16 @@ __device__ __forceinline__ void div_fft_tile(const KGeo& g, const KBufs& b, int 
         }
         v[r] = make_float2(d[0], d[1]);  // z_k = f_{2k} + i f_{2k+1}
     }
-    const bool inB = stockham<false>(v, sm2 + lr * S, sm2 + (R + lr) * S, N, t, b.tw, active);
+    const bool inB = stockham<false, N>(v, sm2 + lr * S, sm2 + (R + lr) * S, t, b.tw, active);
     const float2* Z0 = sm2 + (inB ? R * S : 0);
     // c_m = (1/nPhi)[E_m + e^{-i pi m/N} O_m], E/O from Z_m and conj(Z_{N-m});
-    // pairs (m, N-m) share their inputs.  Items (m, row) with the row fastest.
+    // pairs (m, N-m) share their inputs.  Items (m, row) with the row fastest,
+    // taken by the tile's own R*T threads (the same sequence per thread in a
+    // CTA of any width, so a sphere's spectrum is bit-identical alone and in
+    // a batch of larger spheres).
     const float scale = 1.0f / (float)np;
-    const int nthr = blockDim.x;
-    for (int q = tid; q < (N / 2 + 1) * R; q += nthr) {
+    if (!active) return;
+    for (int q = tid; q < (N / 2 + 1) * R; q += R * T) {
         const int r2 = q & (R - 1), m = q >> lgR;
         const int jj = blk * R + r2;
         const float2* Z = Z0 + r2 * S;
@@ -482,12 +488,49 @@ __device__ __forceinline__ void div_fft_tile(const KGeo& g, const KBufs& b, int 
     }
 }
 
+// Runtime dispatch on nTheta (the batched kernels mix sizes).
 template <int MODE>
-__global__ void __launch_bounds__(1024, 2) k_div_fft(KGeo g, KBufs b, int uv_in, int uv_out)
+__device__ __forceinline__ void div_fft_tile(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int blk,
+                                             int tid, float2* sm2)
+{
+    switch (g.nt) {
+    case 32: div_fft_tile_n<MODE, 32>(g, b, uv_in, uv_out, blk, tid, sm2); break;
+    case 64: div_fft_tile_n<MODE, 64>(g, b, uv_in, uv_out, blk, tid, sm2); break;
+    case 128: div_fft_tile_n<MODE, 128>(g, b, uv_in, uv_out, blk, tid, sm2); break;
+    case 256: div_fft_tile_n<MODE, 256>(g, b, uv_in, uv_out, blk, tid, sm2); break;
+    case 512: div_fft_tile_n<MODE, 512>(g, b, uv_in, uv_out, blk, tid, sm2); break;
+    case 1024: div_fft_tile_n<MODE, 1024>(g, b, uv_in, uv_out, blk, tid, sm2); break;
+    default: div_fft_tile_n<MODE, 2048>(g, b, uv_in, uv_out, blk, tid, sm2); break;
+    }
+}
+
+// resident CTAs per SM the row-FFT kernels are compiled for: a full SM of
+// threads for the 512- and 1024-thread CTAs, four of the 256-thread ones
+__host__ __device__ constexpr int fft_min_ctas(int nt) { return fft_threads(nt) >= 512 ? 2048 / fft_threads(nt) : 4; }
+
+template <int MODE, int N>
+__global__ void __launch_bounds__(fft_threads(N), fft_min_ctas(N)) k_div_fft(KGeo g, KBufs b, int uv_in, int uv_out)
 {
     pdl_wait();
     extern __shared__ float2 sm2[];
-    div_fft_tile<MODE>(g, b, uv_in, uv_out, blockIdx.x, threadIdx.x, sm2);
+    div_fft_tile_n<MODE, N>(g, b, uv_in, uv_out, blockIdx.x, threadIdx.x, sm2);
+}
+
+using RowFftKernel = void (*)(KGeo, KBufs, int, int);
+
+// the instance of k_div_fft for nTheta = nt
+template <int MODE>
+inline RowFftKernel div_fft_kernel(int nt)
+{
+    switch (nt) {
+    case 32: return k_div_fft<MODE, 32>;
+    case 64: return k_div_fft<MODE, 64>;
+    case 128: return k_div_fft<MODE, 128>;
+    case 256: return k_div_fft<MODE, 256>;
+    case 512: return k_div_fft<MODE, 512>;
+    case 1024: return k_div_fft<MODE, 1024>;
+    default: return k_div_fft<MODE, 2048>;
+    }
 }
 
 // ------------------------------------------------------------- mode solve
@@ -773,83 +816,70 @@ __host__ __device__ inline size_t s64_smem(int nt)
     const int th = s64_threads(nt);
     return sizeof(float2) * (size_t)(nt + th) + sizeof(double2) * 2 * (size_t)th;
 }
-// the same with the mode's multiplier table staged in front (k_solve64)
-__host__ __device__ inline size_t s64_smem_staged(int nt) { return sizeof(double) * s64_stride(nt) + s64_smem(nt); }
-inline size_t s64_smem_staged_max()
-{
-    size_t m = 0;
-    for (int nt = 32; nt <= 2048; nt *= 2) m = s64_smem_staged(nt) > m ? s64_smem_staged(nt) : m;
-    return m;
-}
-
-// bytes (a multiple of 16, both addresses 16-byte aligned) copied global ->
-// shared by the CTA with 16-byte cp.async, all issued before the wait, which
-// waits for this thread's own copies; the caller synchronises the CTA.
-__device__ __forceinline__ void copy_async_g2s(void* dst, const void* src, size_t bytes, int t)
-{
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    const char* sp = static_cast<const char*>(src);
-    for (size_t o = (size_t)t * 16; o < bytes; o += (size_t)blockDim.x * 16)
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d + (unsigned)o), "l"(sp + o) : "memory");
-    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
-}
-
 // FP64 solve of mode m: every thread of the CTA calls it (it synchronises);
-// threads t >= nTheta/P own no rows.  STAGED: the mode's multiplier table is
-// first copied into shared memory (s64_smem_staged bytes), so the
-// reduction's per-level multipliers are shared-memory reads rather than a
-// global round trip per level.
-template <int P, bool STAGED>
+// threads t >= nTheta/P own no rows.  The mode's multiplier table is
+// requested into L1 up front, so the reduction's per-level reads do not each
+// wait a global round trip.  COMP: 0 or 1 solves only the real or the
+// imaginary part of the right-hand side (the matrix is real, so the two are
+// independent systems: two CTAs on two SMs share the FP64 work of a mode,
+// which on GB300 is bound by the FP64 pipe of the SM), 2 both.
+template <int P, int COMP>
 __device__ void solve_mode64(const KGeo& g, const KBufs& b, int m, unsigned char* smraw, int t)
 {
+    constexpr int NC = COMP == 2 ? 2 : 1;
     const int n = g.nt, TH = n / P, R = 2 * TH;
     const bool active = t < TH;
     const double* tb = b.s64 + (size_t)(m - 1) * s64_stride(n);
-    if (STAGED) {
-        double* st = reinterpret_cast<double*>(smraw);
-        copy_async_g2s(st, tb, sizeof(double) * s64_stride(n), t);
-        tb = st;
-        smraw += sizeof(double) * s64_stride(n);
+    {
+        const char* p = reinterpret_cast<const char*>(tb);
+        for (size_t o = (size_t)t * 128; o < sizeof(double) * s64_stride(n); o += (size_t)blockDim.x * 128)
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(p + o));
     }
     const double *dn = tb, *up = tb + n, *bA = tb + 2 * n, *bC = tb + 3 * n, *bInv = tb + 4 * n;
     const double *rF = tb + 5 * n, *pl = rF + S64_TH, *ph = pl + S64_L * S64_R, *pinv = ph + S64_L * S64_R;
-    auto ld = [](const double* p) { return STAGED ? *p : __ldg(p); };
+    auto ld = [](const double* p) { return __ldg(p); };
     const float2* __restrict__ col = b.spec + (size_t)(m - 1) * n;
     float2* __restrict__ sol = b.sol + (size_t)(m - 1) * n;
-    float2* cs = reinterpret_cast<float2*>(smraw);             // n + TH slots
-    double2* xs = reinterpret_cast<double2*>(cs + n + TH);     // 2 TH
+    float2* cs = reinterpret_cast<float2*>(smraw);          // n + TH slots
+    double* xs = reinterpret_cast<double*>(cs + n + TH);    // NC * R: component c at xs + c * R
     stage_column(cs, col, n, P, t);
     __syncthreads();
     const int f = t * P;
-    double Dr[P], Di[P];
-    double Fr = 0, Fi = 0, Lr = 0, Li = 0;
+    double D[NC][P];
+    double F[NC], L[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) F[c] = L[c] = 0.0;
     if (active) {
 #pragma unroll
         for (int q = 0; q < P; q++) {
             const float2 d = cs[f + q + t];
-            Dr[q] = -(double)d.x;
-            Di[q] = -(double)d.y;
+            if (NC == 2) {
+                D[0][q] = -(double)d.x;
+                D[NC - 1][q] = -(double)d.y;
+            } else {
+                D[0][q] = -(double)(COMP == 1 ? d.y : d.x);
+            }
         }
 #pragma unroll
         for (int q = 2; q < P; q++) {
             const double r = ld(dn + f + q);
-            Dr[q] = fma(r, Dr[q - 1], Dr[q]);
-            Di[q] = fma(r, Di[q - 1], Di[q]);
+#pragma unroll
+            for (int c = 0; c < NC; c++) D[c][q] = fma(r, D[c][q - 1], D[c][q]);
         }
-        Lr = Dr[P - 1];
-        Li = Di[P - 1];
+#pragma unroll
+        for (int c = 0; c < NC; c++) L[c] = D[c][P - 1];
 #pragma unroll
         for (int q = P - 3; q >= 1; q--) {
             const double r = ld(up + f + q);
-            Dr[q] = fma(r, Dr[q + 1], Dr[q]);
-            Di[q] = fma(r, Di[q + 1], Di[q]);
+#pragma unroll
+            for (int c = 0; c < NC; c++) D[c][q] = fma(r, D[c][q + 1], D[c][q]);
         }
-        Fr = Dr[0];
-        Fi = Di[0];
+#pragma unroll
+        for (int c = 0; c < NC; c++) F[c] = D[c][0];
         if (P >= 3) {
             const double r = ld(rF + t);
-            Fr = fma(r, Dr[1], Fr);
-            Fi = fma(r, Di[1], Fi);
+#pragma unroll
+            for (int c = 0; c < NC; c++) F[c] = fma(r, D[c][1], F[c]);
         }
     }
     // cyclic reduction over the R boundary rows: row 2t = F, 2t + 1 = L
@@ -857,50 +887,60 @@ __device__ void solve_mode64(const KGeo& g, const KBufs& b, int m, unsigned char
     int level = 0;
     for (int s = 1; s < R; s <<= 1, level++) {
         if (active) {
-            xs[iF] = make_double2(Fr, Fi);
-            xs[iL] = make_double2(Lr, Li);
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+                xs[c * R + iF] = F[c];
+                xs[c * R + iL] = L[c];
+            }
         }
         __syncthreads();
         if (active) {
             const double* L0 = pl + level * S64_R;
             const double* H0 = ph + level * S64_R;
-            const double2 z = make_double2(0.0, 0.0);
-            const double2 lf = iF - s >= 0 ? xs[iF - s] : z, hf = iF + s < R ? xs[iF + s] : z;
-            const double2 ll = iL - s >= 0 ? xs[iL - s] : z, hl = iL + s < R ? xs[iL + s] : z;
             const double aF = ld(L0 + iF), cF = ld(H0 + iF), aL = ld(L0 + iL), cL = ld(H0 + iL);
-            Fr = fma(aF, lf.x, fma(cF, hf.x, Fr));
-            Fi = fma(aF, lf.y, fma(cF, hf.y, Fi));
-            Lr = fma(aL, ll.x, fma(cL, hl.x, Lr));
-            Li = fma(aL, ll.y, fma(cL, hl.y, Li));
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+                const double* x = xs + c * R;
+                const double lf = iF - s >= 0 ? x[iF - s] : 0.0, hf = iF + s < R ? x[iF + s] : 0.0;
+                const double ll = iL - s >= 0 ? x[iL - s] : 0.0, hl = iL + s < R ? x[iL + s] : 0.0;
+                F[c] = fma(aF, lf, fma(cF, hf, F[c]));
+                L[c] = fma(aL, ll, fma(cL, hl, L[c]));
+            }
         }
         __syncthreads();
     }
-    if (active) {
-        const double pF = ld(pinv + iF), pL = ld(pinv + iL);
-        const double xfr = Fr * pF, xfi = Fi * pF, xlr = Lr * pL, xli = Li * pL;
-        cs[f + t] = make_float2((float)xfr, (float)xfi);
-        cs[f + P - 1 + t] = make_float2((float)xlr, (float)xli);
+    if (NC == 2) {
+        if (active) {
+            const double pF = ld(pinv + iF), pL = ld(pinv + iL);
+            const double xfr = F[0] * pF, xfi = F[NC - 1] * pF, xlr = L[0] * pL, xli = L[NC - 1] * pL;
+            cs[f + t] = make_float2((float)xfr, (float)xfi);
+            cs[f + P - 1 + t] = make_float2((float)xlr, (float)xli);
 #pragma unroll
-        for (int q = 1; q < P - 1; q++) {
-            const double a = ld(bA + f + q), c = ld(bC + f + q), iv = ld(bInv + f + q);
-            const double xr = fma(a, xfr, fma(c, xlr, Dr[q])) * iv;
-            const double xi = fma(a, xfi, fma(c, xli, Di[q])) * iv;
-            cs[f + q + t] = make_float2((float)xr, (float)xi);
+            for (int q = 1; q < P - 1; q++) {
+                const double a = ld(bA + f + q), c = ld(bC + f + q), iv = ld(bInv + f + q);
+                const double xr = fma(a, xfr, fma(c, xlr, D[0][q])) * iv;
+                const double xi = fma(a, xfi, fma(c, xli, D[NC - 1][q])) * iv;
+                cs[f + q + t] = make_float2((float)xr, (float)xi);
+            }
         }
+        __syncthreads();
+        store_column(sol, cs, n, P, t);
+        return;
     }
-    __syncthreads();
-    store_column(sol, cs, n, P, t);
+    if (!active) return;
+    // one component: its float of each solution entry
+    float* __restrict__ sc = reinterpret_cast<float*>(sol) + (COMP == 1 ? 1 : 0);
+    const double pF = ld(pinv + iF), pL = ld(pinv + iL);
+    const double xf = F[0] * pF, xl = L[0] * pL;
+    sc[2 * f] = (float)xf;
+    sc[2 * (f + P - 1)] = (float)xl;
+#pragma unroll
+    for (int q = 1; q < P - 1; q++) {
+        const double a = ld(bA + f + q), c = ld(bC + f + q), iv = ld(bInv + f + q);
+        sc[2 * (f + q)] = (float)(fma(a, xf, fma(c, xl, D[0][q])) * iv);
+    }
 }
 
-__device__ __forceinline__ void solve_mode64_any(const KGeo& g, const KBufs& b, int m, unsigned char* sm, int t)
-{
-    switch (g.nt / s64_threads(g.nt)) {
-    case 2: solve_mode64<2, false>(g, b, m, sm, t); break;
-    case 4: solve_mode64<4, false>(g, b, m, sm, t); break;
-    case 8: solve_mode64<8, false>(g, b, m, sm, t); break;
-    default: solve_mode64<16, false>(g, b, m, sm, t); break;
-    }
-}
 
 // FP32 rows per thread of the mode solve.
 __host__ __device__ inline int solve_rows(int nt) { return nt >= 256 ? nt / SOLVE_THREADS : 1; }
@@ -932,56 +972,63 @@ inline size_t solve_smem_max()
     return m;
 }
 
-// Mode blk + 1: FP64 when blk < nfp64, otherwise FP32 with P rows
-// per thread (P is a runtime value here; the batched kernels mix sizes).
+// Solve tile blk of a sphere (nt + nfp64 tiles): tiles 0 .. 2 nfp64 - 1 are
+// the FP64 modes, one component each (tile 2(m-1) + c: mode m, component
+// c); the rest the FP32 modes nfp64 + 1 .. nt with P rows per thread (P is a
+// runtime value here; the batched kernels mix sizes).
 __device__ __forceinline__ void solve_tile_p(const KGeo& g, const KBufs& b, int nfp64, int blk, int tid,
                                              unsigned char* smraw, int P)
 {
-    if (blk < nfp64) {  // FP64 mode
-        solve_mode64_any(g, b, blk + 1, smraw, tid);
+    if (blk < 2 * nfp64) {
+        const int m = (blk >> 1) + 1;
+        const int P64 = g.nt / s64_threads(g.nt);
+        if (blk & 1) {
+            switch (P64) {
+            case 2: solve_mode64<2, 1>(g, b, m, smraw, tid); break;
+            case 4: solve_mode64<4, 1>(g, b, m, smraw, tid); break;
+            case 8: solve_mode64<8, 1>(g, b, m, smraw, tid); break;
+            default: solve_mode64<16, 1>(g, b, m, smraw, tid); break;
+            }
+        } else {
+            switch (P64) {
+            case 2: solve_mode64<2, 0>(g, b, m, smraw, tid); break;
+            case 4: solve_mode64<4, 0>(g, b, m, smraw, tid); break;
+            case 8: solve_mode64<8, 0>(g, b, m, smraw, tid); break;
+            default: solve_mode64<16, 0>(g, b, m, smraw, tid); break;
+            }
+        }
         return;
     }
+    const int m = blk - nfp64 + 1;
     switch (P) {
-    case 1: solve_mode32<1>(g, b, blk + 1, smraw, tid); break;
-    case 2: solve_mode32<2>(g, b, blk + 1, smraw, tid); break;
-    case 4: solve_mode32<4>(g, b, blk + 1, smraw, tid); break;
-    case 8: solve_mode32<8>(g, b, blk + 1, smraw, tid); break;
-    default: solve_mode32<16>(g, b, blk + 1, smraw, tid); break;
+    case 1: solve_mode32<1>(g, b, m, smraw, tid); break;
+    case 2: solve_mode32<2>(g, b, m, smraw, tid); break;
+    case 4: solve_mode32<4>(g, b, m, smraw, tid); break;
+    case 8: solve_mode32<8>(g, b, m, smraw, tid); break;
+    default: solve_mode32<16>(g, b, m, smraw, tid); break;
     }
 }
 
+// All mode solves of a step in one launch: CTAs 0 .. 2 nfp64 - 1 take the
+// FP64 modes, one component of the right-hand side each (CTA 2(m-1) + c:
+// mode m, component c), the rest the FP32 modes nfp64 + 1 .. nt.
 template <int P>
-__global__ void __launch_bounds__(SOLVE_THREADS) k_solve(KGeo g, KBufs b, int nfp64)
+__global__ void __launch_bounds__(SOLVE_THREADS, 8) k_solve(KGeo g, KBufs b, int nfp64)
 {
     pdl_wait();
     extern __shared__ __align__(16) unsigned char smraw[];
-    if ((int)blockIdx.x < nfp64) {
+    const int blk = blockIdx.x;
+    if (blk < 2 * nfp64) {
         // FP64 rows per thread: nt / s64_threads(nt), which is P for nt >= 256
         // and 2 below
-        solve_mode64<(P < 2 ? 2 : P), false>(g, b, blockIdx.x + 1, smraw, threadIdx.x);
+        constexpr int P64 = P < 2 ? 2 : P;
+        if (blk & 1)
+            solve_mode64<P64, 1>(g, b, (blk >> 1) + 1, smraw, threadIdx.x);
+        else
+            solve_mode64<P64, 0>(g, b, (blk >> 1) + 1, smraw, threadIdx.x);
         return;
     }
-    solve_mode32<P>(g, b, (int)blockIdx.x + 1, smraw, threadIdx.x);
-}
-
-// The step's mode solves as two kernels on parallel branches of the step
-// graph: k_solve64 takes modes 1 .. nfp64 (one CTA each, nt / P64 threads),
-// k_solve32 modes nfp64 + 1 .. nt, so the FP32 kernel carries neither the
-// FP64 code's registers nor its longer CTAs.
-template <int P>
-__global__ void __launch_bounds__(SOLVE_THREADS, 8) k_solve32(KGeo g, KBufs b, int nfp64)
-{
-    pdl_wait();
-    extern __shared__ __align__(16) unsigned char smraw[];
-    solve_mode32<P>(g, b, (int)blockIdx.x + nfp64 + 1, smraw, threadIdx.x);
-}
-
-template <int P64>
-__global__ void __launch_bounds__(S64_TH) k_solve64(KGeo g, KBufs b)
-{
-    pdl_wait();
-    extern __shared__ __align__(16) unsigned char smraw[];
-    solve_mode64<P64, true>(g, b, (int)blockIdx.x + 1, smraw, threadIdx.x);
+    solve_mode32<P>(g, b, blk - nfp64 + 1, smraw, threadIdx.x);
 }
 
 // ---------------------------------------------------- inverse FFT + u update
@@ -993,18 +1040,18 @@ __global__ void __launch_bounds__(S64_TH) k_solve64(KGeo g, KBufs b)
 // spectrum, whose output is z_k = p_{2k} + i p_{2k+1}.  The solution is
 // mode-major (sol[(m-1)*nt + row]); the CTA first stages its R rows' columns
 // in region B with the row index fastest.
-__device__ __forceinline__ void ifft_tile(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int blk, int tid,
-                                          float2* sm2)
+template <int N>
+__device__ __forceinline__ void ifft_tile_n(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int blk, int tid,
+                                            float2* sm2)
 {
-    const int N = g.nt, T = N >> 2, R = fft_rows_per_cta(N), S = fft_stride(N);
-    const int lgT = g.log2nt - 2, lgR = 31 - __clz(R);
+    constexpr int T = N >> 2, R = fft_rows_per_cta(N), S = fft_stride(N);
+    constexpr int lgT = ilog2c(T), lgR = ilog2c(R);
     const int lr = tid >> lgT, t = tid & (T - 1);
     const bool active = lr < R;
     const int j0 = blk * R, j = j0 + lr;
-    const int np = g.np;
-    const int nthr = blockDim.x;
+    constexpr int np = 2 * N;
     float2* stage = sm2 + R * S;
-    for (int q = tid; q < N * R; q += nthr) {
+    for (int q = active ? tid : N * R; q < N * R; q += R * T) {
         const int r2 = q & (R - 1), mi = q >> lgR;
         stage[r2 * S + mi] = __ldg(b.sol + (size_t)mi * N + j0 + r2);
     }
@@ -1027,32 +1074,77 @@ __device__ __forceinline__ void ifft_tile(const KGeo& g, const KBufs& b, int uv_
             v[r] = make_float2(Er - Oi, Ei + Or);
         }
     }
-    const bool inB = stockham<true>(v, sm2 + lr * S, sm2 + (R + lr) * S, N, t, b.tw, active);
+    const bool inB = stockham<true, N>(v, sm2 + lr * S, sm2 + (R + lr) * S, t, b.tw, active);
     if (!active) return;
     const float2* Z = sm2 + (inB ? R * S : 0) + lr * S;
     const float* __restrict__ uf = b.u[uv_in];
     float* __restrict__ uo = b.u[uv_out];
-    const float nhs = __ldg(b.negHs + j);
+    // applyPressurePhi (KaminoCore.cu:740-746) divides by -h sin(theta_j): here
+    // one reciprocal per row, then products
+    const float inhs = __frcp_rn(__ldg(b.negHs + j));
     const size_t row = (size_t)j * np;
+#pragma unroll
     for (int s = t; s < N; s += T) {
         // p_{2s} = zc.x, p_{2s+1} = zc.y; their west neighbours p_{2s-1} = zp.y, p_{2s}
         const float2 zc = Z[fsw(s)], zp = Z[fsw((s - 1) & (N - 1))];
         const float2 uu = ldg2(uf + row + 2 * s);
-        // applyPressurePhi, KaminoCore.cu:740-746
         float2 o;
-        o.x = __fadd_rn(uu.x, __fdiv_rn(__fsub_rn(zc.x, zp.y), nhs));
-        o.y = __fadd_rn(uu.y, __fdiv_rn(__fsub_rn(zc.y, zc.x), nhs));
+        o.x = __fadd_rn(uu.x, __fmul_rn(__fsub_rn(zc.x, zp.y), inhs));
+        o.y = __fadd_rn(uu.y, __fmul_rn(__fsub_rn(zc.y, zc.x), inhs));
         *reinterpret_cast<float2*>(uo + row + 2 * s) = o;
         *reinterpret_cast<float2*>(b.p + row + 2 * s) = zc;
     }
 }
 
-__global__ void __launch_bounds__(1024, 2) k_ifft_u(KGeo g, KBufs b, int uv_in, int uv_out, int write_p)
+__device__ __forceinline__ void ifft_tile(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int blk, int tid,
+                                          float2* sm2)
+{
+    switch (g.nt) {
+    case 32: ifft_tile_n<32>(g, b, uv_in, uv_out, blk, tid, sm2); break;
+    case 64: ifft_tile_n<64>(g, b, uv_in, uv_out, blk, tid, sm2); break;
+    case 128: ifft_tile_n<128>(g, b, uv_in, uv_out, blk, tid, sm2); break;
+    case 256: ifft_tile_n<256>(g, b, uv_in, uv_out, blk, tid, sm2); break;
+    case 512: ifft_tile_n<512>(g, b, uv_in, uv_out, blk, tid, sm2); break;
+    case 1024: ifft_tile_n<1024>(g, b, uv_in, uv_out, blk, tid, sm2); break;
+    default: ifft_tile_n<2048>(g, b, uv_in, uv_out, blk, tid, sm2); break;
+    }
+}
+
+template <int N>
+__global__ void __launch_bounds__(fft_threads(N), fft_min_ctas(N)) k_ifft_u(KGeo g, KBufs b, int uv_in, int uv_out)
 {
     pdl_wait();
     extern __shared__ float2 sm2[];
-    ifft_tile(g, b, uv_in, uv_out, blockIdx.x, threadIdx.x, sm2);
-    (void)write_p;
+    ifft_tile_n<N>(g, b, uv_in, uv_out, blockIdx.x, threadIdx.x, sm2);
+}
+
+// the instance of k_ifft_u for nTheta = nt
+inline RowFftKernel ifft_kernel(int nt)
+{
+    switch (nt) {
+    case 32: return k_ifft_u<32>;
+    case 64: return k_ifft_u<64>;
+    case 128: return k_ifft_u<128>;
+    case 256: return k_ifft_u<256>;
+    case 512: return k_ifft_u<512>;
+    case 1024: return k_ifft_u<1024>;
+    default: return k_ifft_u<2048>;
+    }
+}
+
+// MaxDynamicSharedMemorySize of every row-FFT kernel instance (the bound
+// over all sizes: the attribute belongs to the function, not to a sphere)
+inline cudaError_t set_fft_smem_limits()
+{
+    const int lim = (int)fft_smem_max();
+    cudaError_t e = cudaSuccess;
+    for (int nt = 32; nt <= 2048 && e == cudaSuccess; nt *= 2) {
+        e = cudaFuncSetAttribute(div_fft_kernel<0>(nt), cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(div_fft_kernel<2>(nt), cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(ifft_kernel(nt), cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    }
+    return e;
 }
 
 // applyPressureTheta (KaminoCore.cu:716-721): v -= (p[j+1] - p[j]) / h, for
@@ -1062,12 +1154,12 @@ __device__ __forceinline__ void vgrad_tile(const KGeo& g, const KBufs& b, int uv
     const int idx = q * ELEM_VEC;
     if (idx >= (g.nt - 1) * g.np) return;
     const float4 pn = ldg4(b.p + idx), ps = ldg4(b.p + idx + g.np), v = ldg4(b.v[uv_in] + idx);
-    const float nh = -g.h;
+    const float ninv = -g.invh;  // the division by -h as a product
     float4 o;
-    o.x = __fadd_rn(v.x, __fdiv_rn(__fsub_rn(ps.x, pn.x), nh));
-    o.y = __fadd_rn(v.y, __fdiv_rn(__fsub_rn(ps.y, pn.y), nh));
-    o.z = __fadd_rn(v.z, __fdiv_rn(__fsub_rn(ps.z, pn.z), nh));
-    o.w = __fadd_rn(v.w, __fdiv_rn(__fsub_rn(ps.w, pn.w), nh));
+    o.x = __fadd_rn(v.x, __fmul_rn(__fsub_rn(ps.x, pn.x), ninv));
+    o.y = __fadd_rn(v.y, __fmul_rn(__fsub_rn(ps.y, pn.y), ninv));
+    o.z = __fadd_rn(v.z, __fmul_rn(__fsub_rn(ps.z, pn.z), ninv));
+    o.w = __fadd_rn(v.w, __fmul_rn(__fsub_rn(ps.w, pn.w), ninv));
     *reinterpret_cast<float4*>(b.v[uv_out] + idx) = o;
 }
 

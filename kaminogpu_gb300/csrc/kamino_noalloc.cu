@@ -184,12 +184,12 @@ extern "C" int kamino_projection_noalloc(int n_theta, const float* u_phi, const 
     const size_t solve_smem = kk::solve_smem(nt);
     // same launches as kamino_projection (the divergence from face
     // velocities, the mode solves, the inverse FFT and both gradients)
-    kk::k_div_fft<2><<<nt / rpc, fft_threads, fft_smem, stream>>>(g, b, 0, 1);
+    kk::div_fft_kernel<2>(nt)<<<nt / rpc, fft_threads, fft_smem, stream>>>(g, b, 0, 1);
     if (P == 1)
-        kk::k_solve<1><<<nt, nt, solve_smem, stream>>>(g, b, NOALLOC_FP64_MODES);
+        kk::k_solve<1><<<nt + NOALLOC_FP64_MODES, nt, solve_smem, stream>>>(g, b, NOALLOC_FP64_MODES);
     else
-        kk::k_solve<2><<<nt, nt / 2, solve_smem, stream>>>(g, b, NOALLOC_FP64_MODES);
-    kk::k_ifft_u<<<nt / rpc, fft_threads, fft_smem, stream>>>(g, b, 0, 1, 1);
+        kk::k_solve<2><<<nt + NOALLOC_FP64_MODES, nt / 2, solve_smem, stream>>>(g, b, NOALLOC_FP64_MODES);
+    kk::ifft_kernel(nt)<<<nt / rpc, fft_threads, fft_smem, stream>>>(g, b, 0, 1);
     const int nv = kk::elem_groups((nt - 1) * g.np);
     kk::k_vgrad<<<(nv + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS, kk::ELEM_THREADS, 0, stream>>>(g, b, 0, 1);
     e = cudaGetLastError();

@@ -47,8 +47,6 @@ struct kamino_solver_s {
     KBufs b;
     int device = 0;
     cudaStream_t stream = nullptr;
-    cudaStream_t side = nullptr;  // FP64 mode solves, a parallel branch of the step
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     void* arena = nullptr;
     size_t arena_bytes = 0;
     int cur_uv = 0, cur_r = 0;  // which buffer holds (u, v) and (thickness, particles)
@@ -147,9 +145,6 @@ extern "C" int kamino_destroy(kamino_handle h)
     if (h->arena) cudaFree(h->arena);
     if (h->flush) cudaFree(h->flush);
     if (h->stream) cudaStreamDestroy(h->stream);
-    if (h->side) cudaStreamDestroy(h->side);
-    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
-    if (h->ev_join) cudaEventDestroy(h->ev_join);
     cudaSetDevice(dev0);
     delete h;
     return KAMINO_OK;
@@ -293,9 +288,6 @@ extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
     const size_t s64 = align_up(sizeof(double) * kk::s64_stride(nt) * std::max(h->nfp64, 1));
     size_t total = 9 * field + 2 * spec + 2 * part + 13 * rowf + 4 * rowd + tw + rt + s64;
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&h->arena, total);
     if (e != cudaSuccess) {
         int code = e == cudaErrorMemoryAllocation ? KAMINO_ERR_ALLOC : KAMINO_ERR_CUDA;
@@ -396,16 +388,7 @@ extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
         h->smem_div = kk::fft_smem(nt);
         h->smem_ifft = h->smem_div;
         h->smem_solve = kk::solve_smem(nt);
-        const int smax = (int)kk::s64_smem_staged_max();
-        e = cudaFuncSetAttribute(kk::k_solve64<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(kk::k_solve64<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(kk::k_solve64<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(kk::k_solve64<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
-        if (e != cudaSuccess) break;
-        const int fmax = (int)kk::fft_smem_max();
-        e = cudaFuncSetAttribute(kk::k_div_fft<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, fmax);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(kk::k_div_fft<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, fmax);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(kk::k_ifft_u, cudaFuncAttributeMaxDynamicSharedMemorySize, fmax);
+        e = kk::set_fft_smem_limits();
     } while (0);
     if (e != cudaSuccess) {
         rc = kamino_fail(KAMINO_ERR_CUDA, "kamino_create: %s", cudaGetErrorString(e));
@@ -465,7 +448,7 @@ static int launch_div(kamino_solver_s* h, int uv_in, int uv_out)
 {
     const KGeo& g = h->g;
     const int rpc = kk::fft_rows_per_cta(g.nt);
-    cudaError_t e = kk::launch_pdl(kk::k_div_fft<MODE>, g.nt / rpc, kk::fft_threads(g.nt), h->smem_div, h->stream, g,
+    cudaError_t e = kk::launch_pdl(kk::div_fft_kernel<MODE>(g.nt), g.nt / rpc, kk::fft_threads(g.nt), h->smem_div, h->stream, g,
                                    h->b, uv_in, uv_out);
     return launched("k_div_fft", e);
 }
@@ -474,39 +457,26 @@ static int launch_solve(kamino_solver_s* h)
 {
     const KGeo& g = h->g;
     const int P = kk::solve_rows(g.nt), threads = g.nt / P;
-    const int grid = g.nt;  // blocks [0, nfp64) take the FP64 modes
-    (void)grid;
-    void (*k32)(KGeo, KBufs, int) = nullptr;
-    void (*k64)(KGeo, KBufs) = nullptr;
-    switch (P) {  // FP64 rows per thread: P for nt >= 256, 2 below
-    case 1: k32 = kk::k_solve32<1>, k64 = kk::k_solve64<2>; break;
-    case 2: k32 = kk::k_solve32<2>, k64 = kk::k_solve64<2>; break;
-    case 4: k32 = kk::k_solve32<4>, k64 = kk::k_solve64<4>; break;
-    case 8: k32 = kk::k_solve32<8>, k64 = kk::k_solve64<8>; break;
-    case 16: k32 = kk::k_solve32<16>, k64 = kk::k_solve64<16>; break;
+    void (*k)(KGeo, KBufs, int) = nullptr;
+    switch (P) {
+    case 1: k = kk::k_solve<1>; break;
+    case 2: k = kk::k_solve<2>; break;
+    case 4: k = kk::k_solve<4>; break;
+    case 8: k = kk::k_solve<8>; break;
+    case 16: k = kk::k_solve<16>; break;
     default: return kamino_fail(KAMINO_ERR_INVALID, "no mode solve for %d rows per thread", P);
     }
-    if (h->nfp64 > 0) {  // fork the FP64 modes onto the side stream
-        KCUDA(cudaEventRecord(h->ev_fork, h->stream));
-        KCUDA(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
-        k64<<<h->nfp64, kk::s64_threads(g.nt), kk::s64_smem_staged(g.nt), h->side>>>(g, h->b);
-        if (int rc = launched("k_solve64")) return rc;
-        KCUDA(cudaEventRecord(h->ev_join, h->side));
-    }
-    if (g.nt > h->nfp64) {
-        cudaError_t e = kk::launch_pdl(k32, g.nt - h->nfp64, threads, h->smem_solve, h->stream, g, h->b, h->nfp64);
-        if (int rc = launched("k_solve32", e)) return rc;
-    }
-    if (h->nfp64 > 0) KCUDA(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
-    return KAMINO_OK;
+    // grid: two CTAs per FP64 mode, one per FP32 mode
+    cudaError_t e = kk::launch_pdl(k, g.nt + h->nfp64, threads, h->smem_solve, h->stream, g, h->b, h->nfp64);
+    return launched("k_solve", e);
 }
 
 static int launch_ifft(kamino_solver_s* h, int uv_in, int uv_out)
 {
     const KGeo& g = h->g;
     const int rpc = kk::fft_rows_per_cta(g.nt);
-    cudaError_t e = kk::launch_pdl(kk::k_ifft_u, g.nt / rpc, kk::fft_threads(g.nt), h->smem_ifft, h->stream, g, h->b,
-                                   uv_in, uv_out, 1);
+    cudaError_t e = kk::launch_pdl(kk::ifft_kernel(g.nt), g.nt / rpc, kk::fft_threads(g.nt), h->smem_ifft, h->stream,
+                                   g, h->b, uv_in, uv_out);
     if (int rc = launched("k_ifft_u", e)) return rc;
     int n = kk::elem_groups((g.nt - 1) * g.np);
     e = kk::launch_pdl(kk::k_vgrad, (n + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS, kk::ELEM_THREADS, 0, h->stream, g,
@@ -537,8 +507,8 @@ static int enqueue_step(kamino_solver_s* h, int cu, int cr, cudaEvent_t* ev)
     if (!rc) {
         const KGeo& g = h->g;
         const int rpc = kk::fft_rows_per_cta(g.nt);
-        cudaError_t e = kk::launch_pdl(kk::k_ifft_u, g.nt / rpc, kk::fft_threads(g.nt), h->smem_ifft, h->stream, g,
-                                       h->b, cu, 1 - cu, 1);
+        cudaError_t e = kk::launch_pdl(kk::ifft_kernel(g.nt), g.nt / rpc, kk::fft_threads(g.nt), h->smem_ifft,
+                                       h->stream, g, h->b, cu, 1 - cu);
         rc = launched("k_ifft_u", e);
     }
     mark(5);
@@ -792,8 +762,7 @@ extern "C" int kamino_time_elapsed(kamino_handle h, double* t, int64_t* steps)
     return KAMINO_OK;
 }
 
-// six kernels, plus k_solve64 on the FP64 branch when modes run in FP64
-extern "C" int kamino_launches_per_step(kamino_handle h) { return kNumKernels + (h && h->nfp64 > 0 ? 1 : 0); }
+extern "C" int kamino_launches_per_step(kamino_handle) { return kNumKernels; }
 
 extern "C" int kamino_device_bytes(kamino_handle h, size_t* bytes)
 {

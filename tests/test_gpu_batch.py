@@ -134,3 +134,24 @@ def test_solvers_of_every_size_coexist(kg):
         for key in ("u_phi", "u_theta", "thickness"):
             assert np.array_equal(a[key].view(np.uint32), b[key].view(np.uint32)), (nt, key)
         s.close()
+
+
+@pytest.mark.parametrize("fp64", [0, 4])
+def test_batch_matches_solo_bitwise_large(kg, fp64):
+    """The largest sphere sizes of the served mix (nTheta 512 and 1024)."""
+    from kaminogpu_gb300.batch import Batch
+    spheres = [(1024, 1.0, 31), (512, 0.8, 32)]
+    cfgs = [kg.default_config(n_theta=nt, radius=R, dt=0.002, fp64_modes=fp64) for nt, R, _ in spheres]
+    with Batch(cfgs) as b:
+        for i, (nt, R, seed) in enumerate(spheres):
+            b.load(i, kg.make_initial_state(nt, lmax=16, seed=seed, radius=R))
+        b.step_n(3)
+        for i, (nt, R, seed) in enumerate(spheres):
+            st = kg.make_initial_state(nt, lmax=16, seed=seed, radius=R)
+            with kg.KaminoSolver(config=cfgs[i]) as s:
+                s.load(st)
+                s.step_n(3)
+                want = s.fields()
+            bad = [k for k, f in (("u_phi", kg.U_PHI), ("u_theta", kg.U_THETA), ("thickness", kg.THICKNESS))
+                   if not np.array_equal(b.get_state(i, f).view(np.uint32), want[k].view(np.uint32))]
+            assert not bad, (nt, bad)
