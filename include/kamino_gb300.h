@@ -25,7 +25,7 @@
  *    (KaminoQuantity.cu:3-18).  u_phi and thickness have nTheta rows,
  *    u_theta has nTheta-1 rows, nPhi = 2*nTheta columns.  Particles are
  *    interleaved (phi, theta) float pairs (KaminoParticles.cu:28-30).
- *  - nTheta must be a power of two in [16, 2048]; the reference's cyclic
+ *  - nTheta must be a power of two in [32, 2048]; the reference's cyclic
  *    reduction has the same power-of-two rule (tdm.cu:11-13).
  */
 #ifndef KAMINO_GB300_H
@@ -287,9 +287,19 @@ typedef struct kamino_server_s* kamino_server;
 typedef struct kamino_server_config {
     size_t budget_bytes;      /* admission budget for resident state        */
     int32_t max_resident;     /* slot limit (0 = unlimited)                 */
-    int32_t steps_per_round;  /* steps every resident sphere takes per round */
+    int32_t steps_per_round;  /* steps every batched sphere takes per round  */
     int32_t device;
-    int32_t reserved[5];
+    int32_t solo_n_theta;     /* requests with n_theta >= this run all their
+                                 steps as one-sphere graphs on their own
+                                 stream, concurrently with everything else
+                                 (0 = 512); smaller ones advance together in
+                                 the batched step                            */
+    int32_t solo_slots;       /* solo requests running at once (0 = 2): each
+                                 large sphere's working set is a good part
+                                 of the L2, and too many at once evict each
+                                 other; a solo request waiting for a slot
+                                 does not hold back smaller ones             */
+    int32_t reserved[3];
 } kamino_server_config;
 
 typedef struct kamino_server_stats {

@@ -72,7 +72,9 @@ class KaminoServerConfig(ctypes.Structure):
         ("max_resident", ctypes.c_int32),
         ("steps_per_round", ctypes.c_int32),
         ("device", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 5),
+        ("solo_n_theta", ctypes.c_int32),
+        ("solo_slots", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 3),
     ]
 
 

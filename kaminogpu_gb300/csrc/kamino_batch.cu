@@ -618,6 +618,8 @@ struct Request {
     size_t bytes = 0;
     bool done = false;
     int status = KAMINO_OK;  // KAMINO_ERR_BUDGET for a request that can never fit
+    bool solo = false;       // advanced by its own one-sphere graphs
+    cudaEvent_t finished = nullptr;  // solo: recorded after its last step
 };
 
 } // namespace
@@ -638,13 +640,31 @@ struct kamino_server_s {
     size_t pooled_bytes = 0;  // free handles kept for reuse also hold HBM
     double busy = 0;
     bool dirty = true;
+    // the batched step's round in flight
+    cudaEvent_t round_done = nullptr;
+    bool round_pending = false;
+    double last_poll = 0;  // for busy_seconds
+    std::vector<cudaEvent_t> free_events;
     ~kamino_server_s()
     {
+        cudaDeviceSynchronize();
         eng.release();
-        for (auto& r : resident)
+        for (auto& r : resident) {
             if (r->h) kamino_destroy(r->h);
+            if (r->finished) cudaEventDestroy(r->finished);
+        }
         for (auto& kv : pool)
             for (kamino_handle h : kv.second) kamino_destroy(h);
+        for (cudaEvent_t e : free_events) cudaEventDestroy(e);
+        if (round_done) cudaEventDestroy(round_done);
+    }
+    int solo_n_theta() const { return cfg.solo_n_theta > 0 ? cfg.solo_n_theta : 512; }
+    int solo_slots() const { return cfg.solo_slots > 0 ? cfg.solo_slots : 2; }
+    int solo_running() const
+    {
+        int n = 0;
+        for (auto& r : resident) n += r->solo ? 1 : 0;
+        return n;
     }
     double now() const
     {
@@ -661,6 +681,8 @@ extern "C" int kamino_server_create(const kamino_server_config* cfg, kamino_serv
     if (s->cfg.steps_per_round <= 0) s->cfg.steps_per_round = 10;
     s->t0 = std::chrono::steady_clock::now();
     int rc = s->eng.init(cfg->device);
+    if (!rc && cudaEventCreateWithFlags(&s->round_done, cudaEventDisableTiming) != cudaSuccess)
+        rc = kamino_fail(KAMINO_ERR_CUDA, "kamino_server_create: event");
     if (rc) {
         delete s;
         return rc;
@@ -750,43 +772,88 @@ static bool server_make_room(kamino_server s, int key, size_t need)
     return s->resident_bytes + s->pooled_bytes + need <= s->cfg.budget_bytes;
 }
 
+// Moves a finished request's result to the host and its handle to the pool.
+static int server_retire(kamino_server s, const std::shared_ptr<Request>& r, double t)
+{
+    int rc = kamino_get_state(r->h, KAMINO_U_PHI, r->u.data(), 0);
+    if (!rc) rc = kamino_get_state(r->h, KAMINO_U_THETA, r->v.data(), 0);
+    if (!rc) rc = kamino_get_state(r->h, KAMINO_THICKNESS, r->r.data(), 0);
+    if (rc) return rc;
+    r->done = true;
+    r->done_at = t;
+    s->latencies.push_back(t - r->arrival);
+    s->completed++;
+    s->resident_bytes -= r->bytes;
+    s->pooled_bytes += r->bytes;
+    s->pool[pool_key(r->cfg)].push_back(r->h);
+    r->h = nullptr;
+    if (r->finished) {
+        s->free_events.push_back(r->finished);
+        r->finished = nullptr;
+    }
+    return KAMINO_OK;
+}
+
+// One turn of the request loop; never waits for the device.
+//  1. solo requests whose last step has finished, and batched ones whose
+//     steps are done once the round in flight has finished, are retired;
+//  2. queued requests whose arrival time has passed are admitted FIFO while
+//     their state fits the budget (and the slot limit): a solo request gets
+//     all its steps launched at once on its handle's stream, a batched one
+//     joins the next round;
+//  3. if no round is in flight, the batched spheres take a round of
+//     min(steps_per_round, fewest steps left) steps.
 extern "C" int kamino_server_poll(kamino_server s, int* n_completed)
 {
     if (!s) return kamino_fail(KAMINO_ERR_INVALID, "null server");
     Engine& e = s->eng;
     BCUDA(cudaSetDevice(e.device));
-    BCUDA(cudaStreamSynchronize(e.stream));  // the previous round is done
     const double t = s->now();
+    if (!s->resident.empty()) s->busy += t - s->last_poll;
+    s->last_poll = t;
     int done_now = 0;
-    // retire finished requests
+    if (s->round_pending) {
+        cudaError_t q = cudaEventQuery(s->round_done);
+        if (q == cudaSuccess) {
+            s->round_pending = false;
+        } else if (q != cudaErrorNotReady) {
+            return kamino_fail(KAMINO_ERR_CUDA, "batched round: %s", cudaGetErrorString(q));
+        }
+    }
     for (size_t i = 0; i < s->resident.size();) {
-        auto& r = s->resident[i];
-        if (r->remaining > 0) {
+        auto r = s->resident[i];
+        bool finished = false;
+        if (r->solo) {
+            cudaError_t q = cudaEventQuery(r->finished);
+            if (q != cudaSuccess && q != cudaErrorNotReady)
+                return kamino_fail(KAMINO_ERR_CUDA, "request %lld: %s", (long long)r->id, cudaGetErrorString(q));
+            finished = q == cudaSuccess;
+        } else {
+            finished = r->remaining == 0 && !s->round_pending;
+        }
+        if (!finished) {
             i++;
             continue;
         }
-        int rc = kamino_get_state(r->h, KAMINO_U_PHI, r->u.data(), 0);
-        if (!rc) rc = kamino_get_state(r->h, KAMINO_U_THETA, r->v.data(), 0);
-        if (!rc) rc = kamino_get_state(r->h, KAMINO_THICKNESS, r->r.data(), 0);
+        int rc = server_retire(s, r, t);
         if (rc) return rc;
-        r->done = true;
-        r->done_at = t;
-        s->latencies.push_back(t - r->arrival);
-        s->completed++;
         done_now++;
-        s->resident_bytes -= r->bytes;
-        s->pooled_bytes += r->bytes;
-        s->pool[pool_key(r->cfg)].push_back(r->h);
-        r->h = nullptr;
+        if (!r->solo) s->dirty = true;
         s->resident[i] = s->resident.back();
         s->resident.pop_back();
-        s->dirty = true;
     }
-    // admit queued requests (FIFO, arrival time reached) while they fit
-    while (!s->queue.empty()) {
-        auto r = s->queue.front();
+    // admit queued requests (FIFO, arrival time reached) while they fit; a
+    // solo request waiting for a solo slot is passed over, not waited for
+    int solo_free = s->solo_slots() - s->solo_running();
+    for (auto qi = s->queue.begin(); qi != s->queue.end();) {
+        auto r = *qi;
         if (r->arrival > t) break;
         if (s->cfg.max_resident > 0 && (int)s->resident.size() >= s->cfg.max_resident) break;
+        const bool solo = r->cfg.n_theta >= s->solo_n_theta();
+        if (solo && solo_free <= 0) {
+            ++qi;
+            continue;
+        }
         size_t need = 0;
         int rc = server_device_bytes(s, r->cfg, &need);
         if (rc) return rc;
@@ -795,7 +862,7 @@ extern "C" int kamino_server_poll(kamino_server s, int* n_completed)
             r->done = true;
             r->status = KAMINO_ERR_BUDGET;
             r->done_at = t;
-            s->queue.pop_front();
+            s->queue.erase(qi);
             return kamino_fail(KAMINO_ERR_BUDGET, "request %lld needs %zu bytes, budget %zu", (long long)r->id, need,
                                s->cfg.budget_bytes);
         }
@@ -811,14 +878,34 @@ extern "C" int kamino_server_poll(kamino_server s, int* n_completed)
             if (!server_make_room(s, pool_key(r->cfg), need)) break;
             rc = kamino_create(&r->cfg, &h);
         }
-        // every resident sphere advances together, so the new one joins at
-        // the engine's buffer parity before its state is written
-        if (!rc) rc = kamino_internal_set_counters(h, e.cu, e.cr, 0, 0.0);
+        r->solo = solo;
+        // a batched sphere joins at the batched step's buffer parity before
+        // its state is written (every batched sphere advances together)
+        if (!rc && !r->solo) rc = kamino_internal_set_counters(h, e.cu, e.cr, 0, 0.0);
         if (!rc) rc = kamino_set_state(h, KAMINO_U_PHI, r->u.data(), 0);
         if (!rc) rc = kamino_set_state(h, KAMINO_U_THETA, r->v.data(), 0);
         if (!rc) rc = kamino_set_state(h, KAMINO_THICKNESS, r->r.data(), 0);
+        if (!rc && r->solo) {
+            if (!s->free_events.empty()) {
+                r->finished = s->free_events.back();
+                s->free_events.pop_back();
+            } else if (cudaEventCreateWithFlags(&r->finished, cudaEventDisableTiming) != cudaSuccess) {
+                rc = kamino_fail(KAMINO_ERR_CUDA, "request event");
+            }
+            if (!rc) rc = kamino_step_n(h, r->remaining);
+            if (!rc && cudaEventRecord(r->finished, kamino_internal_stream(h)) != cudaSuccess)
+                rc = kamino_fail(KAMINO_ERR_CUDA, "request event record");
+            if (!rc) {
+                s->cell_steps += (int64_t)r->remaining * r->cfg.n_theta * 2 * r->cfg.n_theta;
+                r->remaining = 0;
+            }
+        }
         if (rc) {
             if (h) kamino_destroy(h);
+            if (r->finished) {
+                cudaEventDestroy(r->finished);
+                r->finished = nullptr;
+            }
             return rc;
         }
         r->h = h;
@@ -826,26 +913,36 @@ extern "C" int kamino_server_poll(kamino_server s, int* n_completed)
         s->resident_bytes += need;
         s->peak_bytes = std::max(s->peak_bytes, s->resident_bytes);
         s->resident.push_back(r);
-        s->queue.pop_front();
-        s->dirty = true;
+        qi = s->queue.erase(qi);
+        if (r->solo)
+            solo_free--;
+        else
+            s->dirty = true;
     }
-    if (!s->resident.empty()) {
+    if (!s->round_pending) {
         int steps = s->cfg.steps_per_round;
-        for (auto& r : s->resident) steps = std::min(steps, (int)r->remaining);
-        if (steps > 0) {
+        bool any = false;
+        for (auto& r : s->resident)
+            if (!r->solo) {
+                any = true;
+                steps = std::min(steps, (int)r->remaining);
+            }
+        if (any && steps > 0) {
             if (s->dirty) {
                 e.hs.clear();
-                for (auto& r : s->resident) e.hs.push_back(r->h);
+                for (auto& r : s->resident)
+                    if (!r->solo) e.hs.push_back(r->h);
                 int rc = e.rebuild();
                 if (rc) return rc;
                 s->dirty = false;
             }
-            const double t1 = s->now();
             int rc = e.step_n(steps);
             if (rc) return rc;
-            for (auto& r : s->resident) r->remaining -= steps;
+            BCUDA(cudaEventRecord(s->round_done, e.stream));
+            s->round_pending = true;
+            for (auto& r : s->resident)
+                if (!r->solo) r->remaining -= steps;
             s->cell_steps += (int64_t)steps * e.cells;
-            s->busy += s->now() - t1;
         }
     }
     if (n_completed) *n_completed = done_now;

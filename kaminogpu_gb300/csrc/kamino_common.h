@@ -4,6 +4,7 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <cuda_runtime.h>
 #include <vector_types.h>
 
 #include "../../include/kamino_gb300.h"
@@ -36,6 +37,8 @@ int kamino_internal_set_counters(kamino_handle h, int cur_uv, int cur_r, int64_t
 // Re-targets a handle of the same nTheta to a new radius / dt / flags and
 // zeroes its state, so pooled device memory can serve a new request.
 int kamino_internal_reset(kamino_handle h, const kamino_config* cfg);
+// The handle's own stream (its steps and copies are ordered on it).
+cudaStream_t kamino_internal_stream(kamino_handle h);
 
 #define KAMINO_PI_D 3.14159265358979323846   /* M_PI  (KaminoHeader.cuh:26) */
 #define KAMINO_2PI_D 6.28318530717958647692  /* M_2PI (KaminoHeader.cuh:27) */

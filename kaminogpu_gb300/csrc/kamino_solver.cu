@@ -715,6 +715,8 @@ int kamino_internal_set_counters(kamino_handle h, int cur_uv, int cur_r, int64_t
     return KAMINO_OK;
 }
 
+cudaStream_t kamino_internal_stream(kamino_handle h) { return h ? h->stream : nullptr; }
+
 int kamino_internal_reset(kamino_handle h, const kamino_config* cfg)
 {
     int rc = check_handle(h);

@@ -1,6 +1,8 @@
 """Batched and served forms on the GPU.  The batched persistent kernels run
 the same per-tile device code as the one-sphere kernels, so every sphere's
 fields must be bit-identical alone, in a batch, and in the server's mix."""
+import time
+
 import numpy as np
 import pytest
 
@@ -69,10 +71,9 @@ def test_server_results_same_alone_and_in_the_mix(kg, orc):
         # staggered arrivals: later requests join while earlier ones run
         reqs.append((srv.submit(cfg, st, steps, arrival=srv.now() + 0.002 * k), nt, seed, steps))
     done = 0
-    for _ in range(10000):
+    deadline = time.time() + 120
+    while done < len(plan) and time.time() < deadline:
         done += srv.poll()
-        if done == len(plan):
-            break
     assert done == len(plan)
     for rid, nt, seed, steps in reqs:
         got = srv.fetch(rid)
@@ -96,12 +97,11 @@ def test_server_admission_respects_the_budget(kg):
         srv.submit(kg.default_config(n_theta=128, radius=1.0, dt=0.002), st, 12)
     done = 0
     peak_resident = 0
-    for _ in range(10000):
+    deadline = time.time() + 120
+    while done < 6 and time.time() < deadline:
         done += srv.poll()
         s = srv.stats()
         peak_resident = max(peak_resident, s["resident"])
-        if done == 6:
-            break
     s = srv.stats()
     assert done == 6 and peak_resident <= 2 and s["peak_resident_bytes"] <= int(2.5 * one)
     big = kg.make_initial_state(512, lmax=4, seed=1)
