@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(kk::ELEM_THREADS) kb_geo(const KSphere* __rest
     }
 }
 
-__global__ void __launch_bounds__(1024) kb_div_fft(const KSphere* __restrict__ sph, const int2* __restrict__ items,
+__global__ void __launch_bounds__(kk::FFT_MAX_THREADS) kb_div_fft(const KSphere* __restrict__ sph, const int2* __restrict__ items,
                                                   int n, int* counter, int uv_in, int uv_out)
 {
     extern __shared__ float2 sm2[];
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(kk::SOLVE_THREADS) kb_solve(const KSphere* __r
         kk::solve_tile_p(s.g, s.b, s.nfp64, w.y, threadIdx.x, smraw, s.P);
 }
 
-__global__ void __launch_bounds__(1024) kb_ifft(const KSphere* __restrict__ sph, const int2* __restrict__ items,
+__global__ void __launch_bounds__(kk::FFT_MAX_THREADS) kb_ifft(const KSphere* __restrict__ sph, const int2* __restrict__ items,
                                                int n, int* counter, int uv_in, int uv_out)
 {
     extern __shared__ float2 sm2[];
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(kk::ELEM_THREADS) kb_vgrad(const KSphere* __re
     } while (0)
 
 struct Shapes {
-    int adv_cta_per_sm = 8, fft_cta_per_sm = 4, solve_cta_per_sm = 8, adv_tiles_per_item = 2;
+    int adv_cta_per_sm = 8, fft_cta_per_sm = 8, solve_cta_per_sm = 8, adv_tiles_per_item = 2;
 };
 
 // A set of handles advanced together.  Owns the device descriptor array, the
@@ -172,7 +172,8 @@ struct Engine {
     int n_items[ST_COUNT] = {};
     size_t item_off[ST_COUNT] = {};
     size_t smem_fft = 0, smem_solve = 0;
-    int fft_block = 256;  // threads of the FFT kernels: the largest sphere's fft_threads
+    int fft_block = 128;  // threads of the FFT kernels: the largest sphere's fft_threads
+    int fft_resident = 1; // FFT CTAs of that size resident per SM (registers, shared memory)
     Shapes shapes;
     int cu = 0, cr = 0;
     cudaGraphExec_t graph[2][2] = {};
@@ -301,6 +302,10 @@ struct Engine {
         BCUDA(cudaFuncSetAttribute(kb_ifft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kk::fft_smem_max()));
         BCUDA(cudaFuncSetAttribute(kb_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)kk::solve_smem_max()));
+        int occ_div = 1, occ_ifft = 1;
+        BCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_div, kb_div_fft, fft_block, smem_fft));
+        BCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ifft, kb_ifft, fft_block, smem_fft));
+        fft_resident = std::max(1, std::min(occ_div, occ_ifft));
         BCUDA(cudaStreamSynchronize(stream));  // host tables go out of scope
         return KAMINO_OK;
     }
@@ -312,7 +317,7 @@ struct Engine {
                                                                    : (st == ST_SOLVE ? shapes.solve_cta_per_sm
                                                                                      : shapes.adv_cta_per_sm));
         // no more CTAs than can be resident (threads, shared memory)
-        if (st == ST_DIV || st == ST_IFFT) per = std::max(1, std::min(per, 2048 / fft_block));
+        if (st == ST_DIV || st == ST_IFFT) per = std::max(1, std::min(per, fft_resident));
 
         return std::max(1, std::min(n_items[st], per * nsm));
     }
@@ -547,7 +552,7 @@ extern "C" int kamino_batch_autotune(kamino_batch b, int reps, int* chosen, int 
     const Shapes base = e.shapes;
     Shapes best = base;
     double best_ms = 1e30;
-    const int adv_opts[] = {4, 8, 16}, fft_opts[] = {2, 4, 8}, solve_opts[] = {4, 8, 16}, tpi_opts[] = {1, 2, 4};
+    const int adv_opts[] = {4, 8, 16}, fft_opts[] = {4, 8, 16}, solve_opts[] = {4, 8, 16}, tpi_opts[] = {1, 2, 4};
     auto trial = [&](const Shapes& s, double* ms) {
         e.shapes = s;
         int r2 = e.rebuild();

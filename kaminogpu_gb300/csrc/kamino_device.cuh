@@ -414,34 +414,12 @@ __device__ __forceinline__ float geo_root(float G, float uPrev, float vPrev)
     return geo_root_fp64(G, uPrev, vPrev);
 }
 
-// ---------------------------------------------------------------- FFT
-// Radix-2 complex FFT of length n (power of two) on one row in shared memory,
-// worked by one warp.  dit(): bit-reversed input, natural output.
+// ------------------------------------------------------- complex product
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
     return make_float2(__fmaf_rn(a.x, b.x, -a.y * b.y), __fmaf_rn(a.x, b.y, a.y * b.x));
 }
 
-template <bool INVERSE>
-__device__ __forceinline__ void fft_dit_warp(float2* x, int n, int log2n, const float2* __restrict__ tw,
-                                             int lane)
-{
-    for (int s = 1; s <= log2n; s++) {
-        const int half = 1 << (s - 1);
-        const int tstep = n >> s;
-        for (int b = lane; b < (n >> 1); b += 32) {
-            const int grp = b >> (s - 1), k = b & (half - 1);
-            const int i = (grp << s) + k, j = i + half;
-            float2 w = __ldg(tw + k * tstep);
-            if (INVERSE) w.y = -w.y;
-            float2 t = cmul(w, x[j]);
-            float2 a = x[i];
-            x[i] = make_float2(a.x + t.x, a.y + t.y);
-            x[j] = make_float2(a.x - t.x, a.y - t.y);
-        }
-        __syncwarp();
-    }
-}
 
 __device__ __forceinline__ int bitrev(int k, int log2n) { return (int)(__brev((unsigned)k) >> (32 - log2n)); }
 

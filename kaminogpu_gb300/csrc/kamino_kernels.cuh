@@ -256,101 +256,139 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_assign(KGeo g, KBufs b, int uv
     if (j < g.nt - 1) b.v[uv_out][idx] = 0.5f * __fadd_rn(__ldg(b.cv + idx), __ldg(b.cv + idx + g.np));
 }
 
-// ------------------------------------------------------------ FFT (Stockham)
+// ------------------------------------------------------------ FFT (rows)
 __device__ __forceinline__ float2 f2add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ float2 ldg2(const float* p) { return __ldg(reinterpret_cast<const float2*>(p)); }
-
-// 4-point DFT in place, kernel e^{-2 pi i/4} = -i (forward) or +i (inverse)
-template <bool INV>
-__device__ __forceinline__ void dft4(float2& a, float2& b, float2& c, float2& d)
+__device__ __forceinline__ float2 shfl2(float2 v, int src, int width)
 {
-    float2 apc = f2add(a, c), amc = f2sub(a, c), bpd = f2add(b, d), bmd = f2sub(b, d);
-    float2 sb = INV ? make_float2(-bmd.y, bmd.x) : make_float2(bmd.y, -bmd.x);
-    a = f2add(apc, bpd);
-    c = f2sub(apc, bpd);
-    b = f2add(amc, sb);
-    d = f2sub(amc, sb);
+    return make_float2(__shfl_sync(0xffffffffu, v.x, src, width), __shfl_sync(0xffffffffu, v.y, src, width));
 }
 
-// Shared memory of the row FFTs.  A CTA transforms R = fft_rows_per_cta(N)
-// latitude rows with N/4 threads each.  Its shared memory is two regions (A,
-// B) of R rows, row stride fft_stride(N) float2.  Inside a row, slot a lives
-// at fsw(a) = a ^ ((a >> 2) & 15), a permutation of every aligned group of 16
-// slots under which the stores and loads of every Stockham stage are free of
-// bank conflicts; the row skew of the stride does the same for the phases in
-// which consecutive lanes walk the R rows of one Fourier mode (the
-// spectrum/solution transposes, whose global accesses then fill whole 32-byte
-// sectors).
-__host__ __device__ constexpr int fft_rows_per_cta(int nt) { return nt >= 2048 ? 2 : (nt >= 256 ? 4 : 1024 / nt); }
-__host__ __device__ constexpr int fft_threads(int nt) { return fft_rows_per_cta(nt) * (nt >> 2); }
-__host__ __device__ constexpr int fft_stride(int nt) { return nt + ((nt == 32 || nt >= 2048) ? 8 : 4); }
+// Row transforms.  The length-N complex FFT of one latitude row (N = nTheta,
+// z_n = f_{2n} + i f_{2n+1}) is worked by a group of L = fft_lanes(N) lanes
+// of one warp, L = 2^floor(log2(N)/2), each lane holding P = N/L points in
+// registers -- the two-pass Cooley-Tukey split N = P x L:
+//   lane l holds x_{l + L r}, r < P;
+//   pass 1 (registers): Y[l][k1] = sum_r x_{l + L r} W_P^{r k1}, then
+//           Y[l][k1] *= W_N^{l k1} (W_n = e^{-2 pi i/n});
+//   transpose through the row's own block of shared memory;
+//   pass 2 (registers): lane l, slot s < P/L takes k1 = l + L s and forms
+//           X_{k1 + P k2} = sum_l' Y[l'][k1] W_L^{l' k2}, k2 < L.
+// Inside a row only __syncwarp orders the work.  A CTA holds R =
+// fft_rows_per_cta(N) rows (4, or 8 for N = 32) so that the mode-major
+// spectrum and solution columns it exchanges with global memory are whole
+// 32-byte sectors (R rows x 8 bytes), staged in shared memory with the row
+// index fastest.  The transpose blocks and the staging area share the
+// dynamic shared memory; a CTA barrier separates their uses.
 __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n >> 1); }
+__host__ __device__ constexpr int brev(int i, int bits)
+{
+    int r = 0;
+    for (int k = 0; k < bits; k++) r |= ((i >> k) & 1) << (bits - 1 - k);
+    return r;
+}
+__host__ __device__ constexpr int fft_lanes(int nt) { return 1 << (ilog2c(nt) / 2); }
+__host__ __device__ constexpr int fft_rows_per_cta(int nt) { return fft_lanes(nt) == 4 ? 8 : 4; }
+__host__ __device__ constexpr int fft_threads(int nt) { return fft_rows_per_cta(nt) * fft_lanes(nt); }
+constexpr int FFT_MAX_THREADS = 128;  // fft_threads of every supported nTheta is at most this
+// Staging of R rows' mode columns: (mode index mi, row r2) at sidx(); the
+// skew mi R/16 puts 16 consecutive modes of one row on distinct bank pairs.
+__host__ __device__ constexpr int fft_stage_len(int nt) { return nt * fft_rows_per_cta(nt) / 16 * 17; }
+template <int R>
+__device__ __forceinline__ int sidx(int mi, int r2) { return mi * R + r2 + ((mi * R) >> 4); }
+// One row's transpose block: P x (L + 1) float2; for L <= 8 (several rows in
+// one 16-lane phase of a 64-bit access) padded to 8 mod 16 float2, so that
+// neighbouring rows' blocks start 16 banks apart.
+__host__ __device__ constexpr int fft_tblock(int nt)
+{
+    return (nt / fft_lanes(nt)) * (fft_lanes(nt) + 1) +
+           (fft_lanes(nt) >= 16 ? 0 : (24 - ((nt / fft_lanes(nt)) * (fft_lanes(nt) + 1)) % 16) % 16);
+}
 __host__ __device__ inline size_t fft_smem(int nt)
 {
-    return sizeof(float2) * 2 * (size_t)fft_rows_per_cta(nt) * fft_stride(nt);
+    const int t = fft_rows_per_cta(nt) * fft_tblock(nt), s = fft_stage_len(nt);
+    return sizeof(float2) * (size_t)(t > s ? t : s);
 }
-__device__ __forceinline__ int fsw(int a) { return a ^ ((a >> 2) & 15); }
 
-// Complex FFT of length N (power of two, >= 32) by T = N/4 threads per row,
-// Stockham autosort: radix-4 stages, then one radix-2 stage when log2 N is
-// odd (N is a template parameter: the stages unroll with constant strides).
-// Thread t enters holding x[t + r T], r = 0..3.  Every thread of the CTA
-// calls it (it synchronises); inactive threads only synchronise.  The
-// transform ends in natural order (swizzled slots) in rowA or rowB; returns
-// true for rowB.  tw[k] = e^{-2 pi i k/N}.
-template <bool INV, int N>
-__device__ __forceinline__ bool stockham(float2 v[4], float2* rowA, float2* rowB, int t,
-                                         const float2* __restrict__ tw, bool active)
+// e^{-2 pi i k/64}, k < 32: the twiddles of the in-register transforms
+__constant__ float2 kW64[32] = {
+    {1.000000000e+00f, 0.000000000e+00f}, {9.951847196e-01f, -9.801714122e-02f}, {9.807852507e-01f, -1.950903237e-01f}, {9.569403529e-01f, -2.902846634e-01f},
+    {9.238795042e-01f, -3.826834261e-01f}, {8.819212914e-01f, -4.713967443e-01f}, {8.314695954e-01f, -5.555702448e-01f}, {7.730104327e-01f, -6.343932748e-01f},
+    {7.071067691e-01f, -7.071067691e-01f}, {6.343932748e-01f, -7.730104327e-01f}, {5.555702448e-01f, -8.314695954e-01f}, {4.713967443e-01f, -8.819212914e-01f},
+    {3.826834261e-01f, -9.238795042e-01f}, {2.902846634e-01f, -9.569403529e-01f}, {1.950903237e-01f, -9.807852507e-01f}, {9.801714122e-02f, -9.951847196e-01f},
+    {0.000000000e+00f, -1.000000000e+00f}, {-9.801714122e-02f, -9.951847196e-01f}, {-1.950903237e-01f, -9.807852507e-01f}, {-2.902846634e-01f, -9.569403529e-01f},
+    {-3.826834261e-01f, -9.238795042e-01f}, {-4.713967443e-01f, -8.819212914e-01f}, {-5.555702448e-01f, -8.314695954e-01f}, {-6.343932748e-01f, -7.730104327e-01f},
+    {-7.071067691e-01f, -7.071067691e-01f}, {-7.730104327e-01f, -6.343932748e-01f}, {-8.314695954e-01f, -5.555702448e-01f}, {-8.819212914e-01f, -4.713967443e-01f},
+    {-9.238795042e-01f, -3.826834261e-01f}, {-9.569403529e-01f, -2.902846634e-01f}, {-9.807852507e-01f, -1.950903237e-01f}, {-9.951847196e-01f, -9.801714122e-02f},
+};
+
+// z W_64^e (forward) or z conj(W_64^e) (inverse), e < 32 a compile-time
+// constant once the transforms are unrolled; e = 0, 8, 16, 24 need no table.
+template <bool INV>
+__device__ __forceinline__ float2 w64mul(float2 z, int e)
 {
-    constexpr int T = N >> 2, LOG2N = ilog2c(N), NR4 = LOG2N / 2;
-    constexpr bool R2 = (LOG2N & 1) != 0;
-    float2* out = rowA;
-    bool inB = false;
+    constexpr float c = 0.70710678118654752f;
+    if (e == 0) return z;
+    if (e == 16) return INV ? make_float2(-z.y, z.x) : make_float2(z.y, -z.x);
+    if (e == 8)
+        return INV ? make_float2(c * (z.x - z.y), c * (z.x + z.y)) : make_float2(c * (z.x + z.y), c * (z.y - z.x));
+    if (e == 24)
+        return INV ? make_float2(-c * (z.x + z.y), c * (z.x - z.y)) : make_float2(c * (z.y - z.x), -c * (z.x + z.y));
+    float2 w = kW64[e];
+    if (INV) w.y = -w.y;
+    return cmul(z, w);
+}
+
+// One radix-2 decimation-in-frequency stage of span H on a[0..M), then the
+// stages below it.
+template <int M, int H, bool INV>
+__device__ __forceinline__ void dif_stages(float2* a)
+{
 #pragma unroll
-    for (int st = 0; st < NR4; st++) {
-        const int Ns = 1 << (2 * st);
-        if (active) {
-            const int k = t & (Ns - 1);
-            if (st > 0) {
-                const int step = N >> (2 * st + 2);
+    for (int base = 0; base < M; base += 2 * H) {
 #pragma unroll
-                for (int r = 1; r < 4; r++) {
-                    float2 w = __ldg(tw + r * k * step);
-                    if (INV) w.y = -w.y;
-                    v[r] = cmul(w, v[r]);
-                }
-            }
-            dft4<INV>(v[0], v[1], v[2], v[3]);
-            const int base = ((t - k) << 2) + k;
-#pragma unroll
-            for (int r = 0; r < 4; r++) out[fsw(base + r * Ns)] = v[r];
+        for (int k = 0; k < H; k++) {
+            const float2 x = a[base + k], y = a[base + k + H];
+            a[base + k] = f2add(x, y);
+            a[base + k + H] = w64mul<INV>(f2sub(x, y), k * (32 / H));
         }
-        __syncthreads();
-        if (st == NR4 - 1 && !R2) return inB;
-        if (active) {
-#pragma unroll
-            for (int r = 0; r < 4; r++) v[r] = out[fsw(t + r * T)];
-        }
-        out = inB ? rowA : rowB;
-        inB = !inB;
     }
-    if (R2) {  // radix-2, Ns = N/2: butterflies t and t + T
-        constexpr int Ns = N / 2;
-        if (active) {
+    if constexpr (H > 1) dif_stages<M, H / 2, INV>(a);
+}
+
+// In-place M-point FFT of registers a[0..M), M <= 64: natural order in,
+// a[brev(k)] = X_k out.
+template <int M, bool INV>
+__device__ __forceinline__ void fft_regs(float2* a)
+{
+    if constexpr (M > 1) dif_stages<M, M / 2, INV>(a);
+}
+
+// The row FFT proper (see above): a[] holds x_{l + L r} in a[r] on entry and
+// X_{k1 + P k2}, k1 = l + L s, in a[s L + brev(k2)] on exit.  tb is the
+// row's transpose block; tw[k] = W_N^k.
+template <int N, bool INV>
+__device__ __forceinline__ void row_fft(float2* a, float2* tb, int l, const float2* __restrict__ tw)
+{
+    constexpr int L = fft_lanes(N), P = N / L, S = P / L, LGP = ilog2c(P);
+    fft_regs<P, INV>(a);
 #pragma unroll
-            for (int q = 0; q < 2; q++) {
-                const int idx = t + q * T;
-                float2 w = __ldg(tw + idx);
-                if (INV) w.y = -w.y;
-                float2 y = cmul(w, v[q + 2]);
-                out[fsw(idx)] = f2add(v[q], y);
-                out[fsw(idx + Ns)] = f2sub(v[q], y);
-            }
-        }
-        __syncthreads();
+    for (int i = 1; i < P; i++) {  // register i holds Y[l][brev(i)]; i = 0 has W = 1
+        float2 w = __ldg(tw + l * brev(i, LGP));
+        if (INV) w.y = -w.y;
+        a[i] = cmul(a[i], w);
     }
-    return inB;
+#pragma unroll
+    for (int i = 0; i < P; i++) tb[brev(i, LGP) * (L + 1) + l] = a[i];
+    __syncwarp();
+#pragma unroll
+    for (int s = 0; s < S; s++) {
+#pragma unroll
+        for (int q = 0; q < L; q++) a[s * L + q] = tb[(l + L * s) * (L + 1) + q];
+    }
+#pragma unroll
+    for (int s = 0; s < S; s++) fft_regs<L, INV>(a + s * L);
 }
 
 // Divergence and forward real FFT of latitude rows.
@@ -359,132 +397,143 @@ __device__ __forceinline__ bool stockham(float2 v[4], float2* rowA, float2* rowB
 // Writes c_m = (1/nPhi) sum_j div_j e^{-i m phi_j}, m = 1..nt, mode-major:
 // spec[(m-1)*nt + row].  c_0 (the dropped m = 0 mode) is never formed.
 // Tile `blk` = rows [blk*R, blk*R + R); every thread of the CTA calls it,
-// threads past R*N/4 only synchronise and help with the spectrum stores.
+// threads past the tile's fft_threads(N) only join its barriers.
 template <int MODE, int N>
 __device__ __forceinline__ void div_fft_tile_n(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int blk,
                                                int tid, float2* sm2)
 {
-    constexpr int T = N >> 2, R = fft_rows_per_cta(N), S = fft_stride(N);
-    constexpr int lgT = ilog2c(T), lgR = ilog2c(R);
-    const int lr = tid >> lgT, t = tid & (T - 1);
-    const bool active = lr < R;
-    const int j = blk * R + lr;
-    constexpr int np = 2 * N, mask = 2 * N - 1;
-    const int lane = tid & 31;
-    const float* __restrict__ cu = b.cu;
-    const float* __restrict__ cv = b.cv;
-    const float* __restrict__ uf = b.u[uv_in];
-    const float* __restrict__ vf = b.v[uv_in];
-    float* __restrict__ uo = b.u[uv_out];
-    float* __restrict__ vo = b.v[uv_out];
-    float fct = 0.0f, sN = 0.0f, sS = 0.0f;
-    size_t row = 0;
+    constexpr int L = fft_lanes(N), P = N / L, S = P / L, R = fft_rows_per_cta(N);
+    constexpr int LGL = ilog2c(L), LGR = ilog2c(R);
+    constexpr int np = 2 * N;
+    const int lr = tid >> LGL, l = tid & (L - 1);
+    const bool active = lr < R;  // whole warps: R L is a multiple of 32
+    const int j0 = blk * R, j = j0 + lr;
+    float2 a[P];
     if (active) {
-        fct = __ldg(b.divf + j);
-        sN = __ldg(b.sinN + j);
-        sS = __ldg(b.sinS + j);
-        row = (size_t)j * np;
-    }
-    const float2 zero = make_float2(0.0f, 0.0f);
-    float2 v[4];
+        const float* __restrict__ src = MODE == 0 ? b.cu : b.u[uv_in];
+        const float* __restrict__ vf = b.v[uv_in];
+        float* __restrict__ uo = b.u[uv_out];
+        float* __restrict__ vo = b.v[uv_out];
+        const float fct = __ldg(b.divf + j), sN = __ldg(b.sinN + j), sS = __ldg(b.sinS + j);
+        const size_t row = (size_t)j * np;
 #pragma unroll
-    for (int r = 0; r < 4; r++) {
-        // this thread's cells i = 2k, 2k + 1; their phi neighbours come from
-        // the adjacent lanes (same row, consecutive k) or, at a warp or row
-        // edge, from a load of their own
-        const int k = t + r * T, i = 2 * k;
-        const float* src = MODE == 0 ? cu : uf;
-        const float2 c = active ? ldg2(src + row + i) : zero;
-        float cl = __shfl_up_sync(0xffffffffu, c.y, 1);
-        float cr = __shfl_down_sync(0xffffffffu, c.x, 1);
-        if (!active) {
-            v[r] = zero;
-            continue;
-        }
-        if (lane == 0 || t == 0) cl = __ldg(src + row + ((i - 1) & mask));
-        if (lane == 31 || t == T - 1) cr = __ldg(src + row + ((i + 2) & mask));
-        float uW[2], uE[2], vN[2], vS[2];
-        if (MODE == 0) {
-            // assignPhiKernel / assignThetaKernel, KaminoCore.cu:531-533, 546-548
-            uW[0] = 0.5f * __fadd_rn(cl, c.x);
-            uE[0] = 0.5f * __fadd_rn(c.x, c.y);
-            uW[1] = uE[0];
-            uE[1] = 0.5f * __fadd_rn(c.y, cr);
-            const float2 cvj = ldg2(cv + row + i);
-            if (j > 0) {
-                const float2 cn = ldg2(cv + row - np + i);
-                vN[0] = 0.5f * __fadd_rn(cn.x, cvj.x);
-                vN[1] = 0.5f * __fadd_rn(cn.y, cvj.y);
-            } else {
-                vN[0] = vN[1] = 0.0f;
-            }
-            if (j < N - 1) {
-                const float2 cs = ldg2(cv + row + np + i);
-                vS[0] = 0.5f * __fadd_rn(cvj.x, cs.x);
-                vS[1] = 0.5f * __fadd_rn(cvj.y, cs.y);
-                *reinterpret_cast<float2*>(vo + row + i) = make_float2(vS[0], vS[1]);
-            } else {
-                vS[0] = vS[1] = 0.0f;
-            }
-            *reinterpret_cast<float2*>(uo + row + i) = make_float2(uW[0], uW[1]);
-        } else {
-            uW[0] = c.x;
-            uE[0] = c.y;
-            uW[1] = c.y;
-            uE[1] = cr;
-            if (j > 0) {
-                const float2 a = ldg2(vf + row - np + i);
-                vN[0] = a.x;
-                vN[1] = a.y;
-            } else {
-                vN[0] = vN[1] = 0.0f;
-            }
-            if (j < N - 1) {
-                const float2 a = ldg2(vf + row + i);
-                vS[0] = a.x;
-                vS[1] = a.y;
-            } else {
-                vS[0] = vS[1] = 0.0f;
-            }
-        }
-        float d[2];
+        for (int r = 0; r < P; r++) a[r] = ldg2(src + row + 2 * (l + L * r));
+        // phi neighbours f_{2n-1}, f_{2n+2} of point n = l + L r come from
+        // lane l -+ 1; at the group's edge from the neighbouring register
+        const int wl = (l - 1) & (L - 1), el = (l + 1) & (L - 1);
+        float wprev = 0.0f, ecur = __shfl_sync(0xffffffffu, a[0].x, el, L);
+        const float east0 = ecur;
+        if (MODE == 0) wprev = __shfl_sync(0xffffffffu, a[P - 1].y, wl, L);
+        // theta-neighbour loads are issued CH registers at a time, so that a
+        // lane keeps 3 CH of them in flight (few warps per SM hold these rows)
+        constexpr int CH = P >= 64 ? 2 : 8;
+        const float2 zero = make_float2(0.0f, 0.0f);
 #pragma unroll
-        for (int e = 0; e < 2; e++) {
-            // fillDivergenceKernel, KaminoCore.cu:625-632
-            float termTheta = __fmul_rn(fct, __fsub_rn(__fmul_rn(vS[e], sS), __fmul_rn(vN[e], sN)));
-            float termPhi = __fmul_rn(fct, __fsub_rn(uE[e], uW[e]));
-            d[e] = __fadd_rn(termTheta, termPhi);
+        for (int r0 = 0; r0 < P; r0 += CH) {
+            float2 vA[CH], vB[CH], vC[CH];  // MODE 0: cv rows j-1, j, j+1; MODE 2: vf rows j-1, j
+#pragma unroll
+            for (int q = 0; q < CH; q++) {
+                const int i = 2 * (l + L * (r0 + q));
+                if (MODE == 0) {
+                    vB[q] = ldg2(b.cv + row + i);
+                    vA[q] = j > 0 ? ldg2(b.cv + row - np + i) : zero;
+                    vC[q] = j < N - 1 ? ldg2(b.cv + row + np + i) : zero;
+                } else {
+                    vA[q] = j > 0 ? ldg2(vf + row - np + i) : zero;
+                    vB[q] = j < N - 1 ? ldg2(vf + row + i) : zero;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < CH; q++) {
+                const int r = r0 + q, i = 2 * (l + L * r);
+                const float2 c = a[r];
+                const float enext = r + 1 < P ? __shfl_sync(0xffffffffu, a[r + 1].x, el, L) : east0;
+                const float cr = l == L - 1 ? enext : ecur;
+                ecur = enext;
+                float uW[2], uE[2], vN[2], vS[2];
+                if (MODE == 0) {
+                    const float wcur = __shfl_sync(0xffffffffu, c.y, wl, L);
+                    const float cl = l == 0 ? wprev : wcur;
+                    wprev = wcur;
+                    // assignPhiKernel / assignThetaKernel, KaminoCore.cu:531-533, 546-548
+                    uW[0] = 0.5f * __fadd_rn(cl, c.x);
+                    uE[0] = 0.5f * __fadd_rn(c.x, c.y);
+                    uW[1] = uE[0];
+                    uE[1] = 0.5f * __fadd_rn(c.y, cr);
+                    if (j > 0) {
+                        vN[0] = 0.5f * __fadd_rn(vA[q].x, vB[q].x);
+                        vN[1] = 0.5f * __fadd_rn(vA[q].y, vB[q].y);
+                    } else {
+                        vN[0] = vN[1] = 0.0f;
+                    }
+                    if (j < N - 1) {
+                        vS[0] = 0.5f * __fadd_rn(vB[q].x, vC[q].x);
+                        vS[1] = 0.5f * __fadd_rn(vB[q].y, vC[q].y);
+                        *reinterpret_cast<float2*>(vo + row + i) = make_float2(vS[0], vS[1]);
+                    } else {
+                        vS[0] = vS[1] = 0.0f;
+                    }
+                    *reinterpret_cast<float2*>(uo + row + i) = make_float2(uW[0], uW[1]);
+                } else {
+                    uW[0] = c.x;
+                    uE[0] = c.y;
+                    uW[1] = c.y;
+                    uE[1] = cr;
+                    vN[0] = vA[q].x;
+                    vN[1] = vA[q].y;
+                    vS[0] = vB[q].x;
+                    vS[1] = vB[q].y;
+                }
+                float d[2];
+#pragma unroll
+                for (int e = 0; e < 2; e++) {
+                    // fillDivergenceKernel, KaminoCore.cu:625-632
+                    float termTheta = __fmul_rn(fct, __fsub_rn(__fmul_rn(vS[e], sS), __fmul_rn(vN[e], sN)));
+                    float termPhi = __fmul_rn(fct, __fsub_rn(uE[e], uW[e]));
+                    d[e] = __fadd_rn(termTheta, termPhi);
+                }
+                a[r] = make_float2(d[0], d[1]);  // z_n = f_{2n} + i f_{2n+1}
+            }
         }
-        v[r] = make_float2(d[0], d[1]);  // z_k = f_{2k} + i f_{2k+1}
+        row_fft<N, false>(a, sm2 + lr * fft_tblock(N), l, b.tw);
     }
-    const bool inB = stockham<false, N>(v, sm2 + lr * S, sm2 + (R + lr) * S, t, b.tw, active);
-    const float2* Z0 = sm2 + (inB ? R * S : 0);
-    // c_m = (1/nPhi)[E_m + e^{-i pi m/N} O_m], E/O from Z_m and conj(Z_{N-m});
-    // pairs (m, N-m) share their inputs.  Items (m, row) with the row fastest,
-    // taken by the tile's own R*T threads (the same sequence per thread in a
-    // CTA of any width, so a sphere's spectrum is bit-identical alone and in
-    // a batch of larger spheres).
-    const float scale = 1.0f / (float)np;
+    __syncthreads();  // every transpose block is read before the staging reuses it
+    if (active) {
+        // c_m = (1/nPhi)[E_m + e^{-i pi m/N} O_m] with E, O from Z_m and
+        // conj(Z_{N-m}); Z_{N-m} sits in lane L - l (lane 0: its own registers)
+        const float scale = 1.0f / (float)np;
+        const int pl = (L - l) & (L - 1);
+        constexpr int LGLc = LGL;
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+#pragma unroll
+            for (int k2 = 0; k2 < L; k2++) {
+                const float2 za = a[s * L + brev(k2, LGLc)];
+                const float2 zsh = shfl2(a[(S - 1 - s) * L + brev(L - 1 - k2, LGLc)], pl, L);
+                const float2 zown = s == 0 ? a[brev((L - k2) & (L - 1), LGLc)] : a[(S - s) * L + brev(L - 1 - k2, LGLc)];
+                const int m = l + L * s + P * k2;
+                float2 c;
+                int mi;
+                if (s == 0 && k2 == 0 && l == 0) {  // c_N (real): Re Z_0 - Im Z_0
+                    c = make_float2((za.x - za.y) * scale, 0.0f);
+                    mi = N - 1;
+                } else {
+                    const float2 zb = l == 0 ? zown : zsh;
+                    const float2 wa = __ldg(b.rt + m);
+                    const float er = 0.5f * (za.x + zb.x), ei = 0.5f * (za.y - zb.y);
+                    const float orr = 0.5f * (za.y + zb.y), oi = -0.5f * (za.x - zb.x);
+                    c = make_float2((er + wa.x * orr - wa.y * oi) * scale, (ei + wa.x * oi + wa.y * orr) * scale);
+                    mi = m - 1;
+                }
+                sm2[sidx<R>(mi, lr)] = c;
+            }
+        }
+    }
+    __syncthreads();
     if (!active) return;
-    for (int q = tid; q < (N / 2 + 1) * R; q += R * T) {
-        const int r2 = q & (R - 1), m = q >> lgR;
-        const int jj = blk * R + r2;
-        const float2* Z = Z0 + r2 * S;
-        if (m == 0) {  // c_N (real): Re Z_0 - Im Z_0
-            const float2 z0 = Z[0];
-            b.spec[(size_t)(N - 1) * N + jj] = make_float2((z0.x - z0.y) * scale, 0.0f);
-            continue;
-        }
-        const int mb = N - m;
-        const float2 za = Z[fsw(m)], zb = Z[fsw(mb)];
-        const float2 wa = __ldg(b.rt + m), wb = __ldg(b.rt + mb);
-        float er = 0.5f * (za.x + zb.x), ei = 0.5f * (za.y - zb.y);
-        float orr = 0.5f * (za.y + zb.y), oi = -0.5f * (za.x - zb.x);
-        b.spec[(size_t)(m - 1) * N + jj] =
-            make_float2((er + wa.x * orr - wa.y * oi) * scale, (ei + wa.x * oi + wa.y * orr) * scale);
-        if (mb != m)  // (Zb, Za): E' = conj(E), O' = conj(O)
-            b.spec[(size_t)(mb - 1) * N + jj] =
-                make_float2((er + wb.x * orr + wb.y * oi) * scale, (-ei - wb.x * oi + wb.y * orr) * scale);
+    for (int q = tid; q < N * R; q += R * L) {
+        const int r2 = q & (R - 1), mi = q >> LGR;
+        b.spec[(size_t)mi * N + j0 + r2] = sm2[sidx<R>(mi, r2)];
     }
 }
 
@@ -504,12 +553,8 @@ __device__ __forceinline__ void div_fft_tile(const KGeo& g, const KBufs& b, int 
     }
 }
 
-// resident CTAs per SM the row-FFT kernels are compiled for: a full SM of
-// threads for the 512- and 1024-thread CTAs, four of the 256-thread ones
-__host__ __device__ constexpr int fft_min_ctas(int nt) { return fft_threads(nt) >= 512 ? 2048 / fft_threads(nt) : 4; }
-
 template <int MODE, int N>
-__global__ void __launch_bounds__(fft_threads(N), fft_min_ctas(N)) k_div_fft(KGeo g, KBufs b, int uv_in, int uv_out)
+__global__ void __launch_bounds__(fft_threads(N)) k_div_fft(KGeo g, KBufs b, int uv_in, int uv_out)
 {
     pdl_wait();
     extern __shared__ float2 sm2[];
@@ -1039,60 +1084,90 @@ __global__ void __launch_bounds__(SOLVE_THREADS, 8) k_solve(KGeo g, KBufs b, int
 // Y_m = (X_m + X_{m+nt}) + i (X_m - X_{m+nt}) e^{i pi m/nt}, X the Hermitian
 // spectrum, whose output is z_k = p_{2k} + i p_{2k+1}.  The solution is
 // mode-major (sol[(m-1)*nt + row]); the CTA first stages its R rows' columns
-// in region B with the row index fastest.
+// with the row index fastest.
 template <int N>
 __device__ __forceinline__ void ifft_tile_n(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int blk, int tid,
                                             float2* sm2)
 {
-    constexpr int T = N >> 2, R = fft_rows_per_cta(N), S = fft_stride(N);
-    constexpr int lgT = ilog2c(T), lgR = ilog2c(R);
-    const int lr = tid >> lgT, t = tid & (T - 1);
+    constexpr int L = fft_lanes(N), P = N / L, S = P / L, R = fft_rows_per_cta(N);
+    constexpr int LGL = ilog2c(L), LGR = ilog2c(R);
+    constexpr int np = 2 * N;
+    const int lr = tid >> LGL, l = tid & (L - 1);
     const bool active = lr < R;
     const int j0 = blk * R, j = j0 + lr;
-    constexpr int np = 2 * N;
-    float2* stage = sm2 + R * S;
-    for (int q = active ? tid : N * R; q < N * R; q += R * T) {
-        const int r2 = q & (R - 1), mi = q >> lgR;
-        stage[r2 * S + mi] = __ldg(b.sol + (size_t)mi * N + j0 + r2);
-    }
-    __syncthreads();
-    float2 v[4];
+    // each thread moves P of the tile's N R values: all loads first
+    float2 a[P];
     if (active) {
-        const float2* U = stage + lr * S;  // U[m-1] = U_m
 #pragma unroll
-        for (int r = 0; r < 4; r++) {
-            const int m = t + r * T;
-            if (m == 0) {
-                float un = U[N - 1].x;  // X_nt = U_nt, real
-                v[r] = make_float2(un, -un);
-                continue;
-            }
-            float2 ua = U[m - 1], ub = U[N - m - 1];  // X_m, and X_{m+nt} = conj(U_{nt-m})
-            float2 ea = __ldg(b.rt + m);
-            float Er = ua.x + ub.x, Ei = ua.y - ub.y, Dr = ua.x - ub.x, Di = ua.y + ub.y;
-            float Or = Dr * ea.x + Di * ea.y, Oi = Di * ea.x - Dr * ea.y;  // D * e^{+i pi m/nt}
-            v[r] = make_float2(Er - Oi, Ei + Or);
+        for (int r = 0; r < P; r++) {
+            const int q = tid + r * R * L, r2 = q & (R - 1), mi = q >> LGR;
+            a[r] = __ldg(b.sol + (size_t)mi * N + j0 + r2);
+        }
+#pragma unroll
+        for (int r = 0; r < P; r++) {
+            const int q = tid + r * R * L, r2 = q & (R - 1), mi = q >> LGR;
+            sm2[sidx<R>(mi, r2)] = a[r];
         }
     }
-    const bool inB = stockham<true, N>(v, sm2 + lr * S, sm2 + (R + lr) * S, t, b.tw, active);
+    __syncthreads();
+    if (active) {
+#pragma unroll
+        for (int r = 0; r < P; r++) {
+            const int m = l + L * r;
+            if (r == 0 && l == 0) {
+                const float un = sm2[sidx<R>(N - 1, lr)].x;  // X_nt = U_nt, real
+                a[r] = make_float2(un, -un);
+                continue;
+            }
+            // X_m = U_m, and X_{m+nt} = conj(U_{nt-m})
+            const float2 ua = sm2[sidx<R>(m - 1, lr)], ub = sm2[sidx<R>(N - m - 1, lr)];
+            const float2 ea = __ldg(b.rt + m);
+            const float Er = ua.x + ub.x, Ei = ua.y - ub.y, Dr = ua.x - ub.x, Di = ua.y + ub.y;
+            const float Or = Dr * ea.x + Di * ea.y, Oi = Di * ea.x - Dr * ea.y;  // D * e^{+i pi m/nt}
+            a[r] = make_float2(Er - Oi, Ei + Or);
+        }
+    }
+    __syncthreads();  // the staging is read before the transpose blocks reuse it
     if (!active) return;
-    const float2* Z = sm2 + (inB ? R * S : 0) + lr * S;
+    row_fft<N, true>(a, sm2 + lr * fft_tblock(N), l, b.tw);
     const float* __restrict__ uf = b.u[uv_in];
     float* __restrict__ uo = b.u[uv_out];
     // applyPressurePhi (KaminoCore.cu:740-746) divides by -h sin(theta_j): here
     // one reciprocal per row, then products
     const float inhs = __frcp_rn(__ldg(b.negHs + j));
     const size_t row = (size_t)j * np;
+    // z_k, k = l + L s + P k2, is in a[s L + brev(k2)]; the west neighbour
+    // p_{2k-1} = Im z_{k-1} comes from lane l - 1, or for l = 0 from lane
+    // L - 1 at the previous (s, k2) in the order below
+    const int wl = (l - 1) & (L - 1);
+    constexpr int LGLc = LGL;
+    float wprev = __shfl_sync(0xffffffffu, a[(S - 1) * L + brev(L - 1, LGLc)].y, wl, L);
+    // u loads in flight per lane: K2C S (whole k2 rows of the register grid)
+    constexpr int K2C = (P >= 64 ? 4 : 8) / S > 0 ? (P >= 64 ? 4 : 8) / S : 1;
+    static_assert(L % K2C == 0, "chunks of k2");
 #pragma unroll
-    for (int s = t; s < N; s += T) {
-        // p_{2s} = zc.x, p_{2s+1} = zc.y; their west neighbours p_{2s-1} = zp.y, p_{2s}
-        const float2 zc = Z[fsw(s)], zp = Z[fsw((s - 1) & (N - 1))];
-        const float2 uu = ldg2(uf + row + 2 * s);
-        float2 o;
-        o.x = __fadd_rn(uu.x, __fmul_rn(__fsub_rn(zc.x, zp.y), inhs));
-        o.y = __fadd_rn(uu.y, __fmul_rn(__fsub_rn(zc.y, zc.x), inhs));
-        *reinterpret_cast<float2*>(uo + row + 2 * s) = o;
-        *reinterpret_cast<float2*>(b.p + row + 2 * s) = zc;
+    for (int k20 = 0; k20 < L; k20 += K2C) {
+        float2 uu[K2C * S];
+#pragma unroll
+        for (int q = 0; q < K2C * S; q++) {
+            const int k = l + L * (q % S) + P * (k20 + q / S);
+            uu[q] = ldg2(uf + row + 2 * k);
+        }
+#pragma unroll
+        for (int q = 0; q < K2C * S; q++) {
+            const int s = q % S, k2 = k20 + q / S;
+            const float2 zc = a[s * L + brev(k2, LGLc)];
+            const float wcur = __shfl_sync(0xffffffffu, zc.y, wl, L);
+            const float zpy = l == 0 ? wprev : wcur;
+            wprev = wcur;
+            const int k = l + L * s + P * k2;
+            float2 o;
+            const float2 u2 = uu[q];
+            o.x = __fadd_rn(u2.x, __fmul_rn(__fsub_rn(zc.x, zpy), inhs));
+            o.y = __fadd_rn(u2.y, __fmul_rn(__fsub_rn(zc.y, zc.x), inhs));
+            *reinterpret_cast<float2*>(uo + row + 2 * k) = o;
+            *reinterpret_cast<float2*>(b.p + row + 2 * k) = zc;
+        }
     }
 }
 
@@ -1111,7 +1186,7 @@ __device__ __forceinline__ void ifft_tile(const KGeo& g, const KBufs& b, int uv_
 }
 
 template <int N>
-__global__ void __launch_bounds__(fft_threads(N), fft_min_ctas(N)) k_ifft_u(KGeo g, KBufs b, int uv_in, int uv_out)
+__global__ void __launch_bounds__(fft_threads(N)) k_ifft_u(KGeo g, KBufs b, int uv_in, int uv_out)
 {
     pdl_wait();
     extern __shared__ float2 sm2[];
