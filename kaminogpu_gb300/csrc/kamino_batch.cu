@@ -41,7 +41,6 @@ struct KSphere {
     int nb_u, nb_v, nb_r, nb_adv;  // advection tiles (u_phi, u_theta, thickness, all incl. particles)
     int nb_elem;                   // tiles of ELEM_THREADS four-cell groups of nt * nPhi
     int nb_fft;                    // row groups of the FFT kernels
-    int P;                         // solve rows per thread
     int nfp64;
     int ref;                       // reference-rounding sampler
 };
@@ -70,7 +69,7 @@ __device__ __forceinline__ bool next_item(int* counter, int n, const int2* __res
     return true;
 }
 
-__global__ void __launch_bounds__(kk::ADV_THREADS) kb_advect(const KSphere* __restrict__ sph,
+__global__ void __launch_bounds__(kk::ADV_THREADS, 8) kb_advect(const KSphere* __restrict__ sph,
                                                               const int2* __restrict__ items, int n, int* counter,
                                                               int cu, int cr, int tiles_per_item)
 {
@@ -120,7 +119,7 @@ __global__ void __launch_bounds__(kk::SOLVE_THREADS) kb_solve(const KSphere* __r
     __shared__ int s_item;
     int2 w;
     while (next_item(counter, n, items, sph, 1, &s, &s_item, &w))
-        kk::solve_tile_p(s.g, s.b, s.nfp64, w.y, threadIdx.x, smraw, s.P);
+        kk::solve_tile(s.g, s.b, s.nfp64, w.y, threadIdx.x, smraw);
 }
 
 __global__ void __launch_bounds__(kk::FFT_MAX_THREADS) kb_ifft(const KSphere* __restrict__ sph, const int2* __restrict__ items,
@@ -243,7 +242,6 @@ struct Engine {
             s.nb_adv = s.nb_u + s.nb_v + s.nb_r + (int)((s.b.npart + kk::ADV_THREADS - 1) / kk::ADV_THREADS);
             s.nb_elem = (kk::elem_groups(s.g.nt * s.g.np) + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS;
             s.nb_fft = s.g.nt / kk::fft_rows_per_cta(s.g.nt);
-            s.P = kk::solve_rows(s.g.nt);
             s.ref = (s.g.flags & KAMINO_F_REFERENCE_ROUNDING) ? 1 : 0;
             host_desc.push_back(s);
             cells += (int64_t)s.g.nt * s.g.np;
@@ -268,7 +266,7 @@ struct Engine {
                 case ST_VGRAD: count = (s.nb_elem + tpi - 1) / tpi; break;
                 case ST_DIV:
                 case ST_IFFT: count = s.nb_fft; break;
-                case ST_SOLVE: count = s.g.nt + s.nfp64; break;  // two tiles per FP64 mode
+                case ST_SOLVE: count = kk::solve_tiles(s.g.nt, s.nfp64); break;
                 }
                 for (int t = 0; t < count; t++) items.push_back(make_int2(i, t));
             }

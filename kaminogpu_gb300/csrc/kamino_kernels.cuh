@@ -31,7 +31,7 @@ using namespace kdev;
 
 constexpr int ADV_THREADS = 256;
 constexpr int ELEM_THREADS = 256;
-constexpr int SOLVE_THREADS = 128;  // threads per Fourier mode in k_solve (nTheta >= 128)
+constexpr int SOLVE_THREADS = 128;  // threads of a k_solve CTA (one tile of Fourier modes)
 
 // Programmatic dependent launch.  The step kernels are launched with
 // programmatic stream serialization (launch_pdl), so a kernel's CTAs can be
@@ -179,8 +179,10 @@ __device__ __forceinline__ void advect_tile(const KGeo& g, const KBufs& b, int s
     b.part[dr][k] = out;
 }
 
+// compiled for eight resident CTAs per SM (32 registers): the gathers are
+// latency-bound, and full occupancy beats the few spilled registers
 template <bool REF>
-__global__ void __launch_bounds__(ADV_THREADS) k_advect(KGeo g, KBufs b, int suv, int duv, int sr, int dr,
+__global__ void __launch_bounds__(ADV_THREADS, 8) k_advect(KGeo g, KBufs b, int suv, int duv, int sr, int dr,
                                                          int nb_u, int nb_v, int nb_r)
 {
     pdl_wait();
@@ -590,17 +592,19 @@ inline RowFftKernel div_fft_kernel(int nt)
 // relative accuracy for every mode; the direct FP32 forms lose about
 // cond(T) ~ nTheta^2/m^2 ulps on the low modes.
 //
-// FP32 modes: SOLVE_THREADS threads per mode, P = nTheta/SOLVE_THREADS rows
-// per thread in registers.  Each thread eliminates inside its block so the
-// interior rows couple only to the block's first and last unknowns; those
-// 2*SOLVE_THREADS rows form a tridiagonal M-matrix solved by parallel cyclic
-// reduction in shared memory.  FP64 modes: the same scheme with multipliers
-// precomputed in FP64 on the host (the matrix is fixed), so the device only
-// runs the right-hand-side recurrences.  The spectrum column and the
-// solution column of a mode (both contiguous, mode-major) pass through
-// shared memory with one pad slot per P rows, so the global accesses are
-// coalesced and each thread's P consecutive rows are read without bank
-// conflicts.
+// FP32 modes (nTheta <= 1024): one warp per mode, P = nTheta/32 rows per
+// lane in registers (solve_warp32).  Each lane eliminates inside its block
+// so the interior rows couple only to the block's first and last unknowns;
+// those 64 rows form a tridiagonal M-matrix solved by parallel cyclic
+// reduction across the lanes (shuffles, no CTA barrier).  nTheta = 2048: the
+// same with SOLVE_THREADS threads of 16 rows per mode and the reduction of
+// the 256 boundary rows in shared memory (solve_mode32).  FP64 modes: the
+// block scheme with multipliers precomputed in FP64 on the host (the matrix
+// is fixed), so the device only runs the right-hand-side recurrences.  The
+// spectrum column and the solution column of a mode (both contiguous,
+// mode-major) pass through shared memory with one pad slot per P rows, so
+// the global accesses are coalesced and each thread's P consecutive rows are
+// read without bank conflicts.
 struct RowF {
     float a, c, s, dr, di;  // couplings (>= 0), dominance (>= 0), right-hand side
 };
@@ -839,6 +843,173 @@ __device__ void solve_mode32(const KGeo& g, const KBufs& b, int m, unsigned char
     store_column(sol, cs, n, P, t);
 }
 
+// Row of a reduced system moved between lanes
+__device__ __forceinline__ RowF shfl_row_up(const RowF& r, int d)
+{
+    RowF o;
+    o.a = __shfl_up_sync(0xffffffffu, r.a, d);
+    o.c = __shfl_up_sync(0xffffffffu, r.c, d);
+    o.s = __shfl_up_sync(0xffffffffu, r.s, d);
+    o.dr = __shfl_up_sync(0xffffffffu, r.dr, d);
+    o.di = __shfl_up_sync(0xffffffffu, r.di, d);
+    return o;
+}
+__device__ __forceinline__ RowF shfl_row_down(const RowF& r, int d)
+{
+    RowF o;
+    o.a = __shfl_down_sync(0xffffffffu, r.a, d);
+    o.c = __shfl_down_sync(0xffffffffu, r.c, d);
+    o.s = __shfl_down_sync(0xffffffffu, r.s, d);
+    o.dr = __shfl_down_sync(0xffffffffu, r.dr, d);
+    o.di = __shfl_down_sync(0xffffffffu, r.di, d);
+    return o;
+}
+
+// FP32 solve of mode m by one warp (nTheta = 32 P <= 1024): lane l owns rows
+// [l P, l P + P) in registers and eliminates inside its block as
+// solve_mode32 does; the 64 boundary rows (first and last of each block) are
+// then reduced by cyclic reduction across the lanes with shuffles, with no
+// CTA barrier anywhere.  P = 1: plain cyclic reduction of the 32 rows.  cs
+// is the warp's staging of the spectrum and solution columns: row r at slot
+// r + r/P, so each lane's P consecutive rows are read without bank conflicts
+// while the global accesses stay coalesced.
+template <int P>
+__device__ __forceinline__ void solve_warp32(const KGeo& g, const KBufs& b, int m, float2* cs, int l)
+{
+    constexpr int n = 32 * P;
+    const float m2 = (float)m * (float)m;
+    const float2* __restrict__ col = b.spec + (size_t)(m - 1) * n;
+    float2* __restrict__ sol = b.sol + (size_t)(m - 1) * n;
+    if constexpr (P == 1) {
+        RowF x;
+        x.a = __ldg(b.lapA + l);
+        x.c = __ldg(b.lapC + l);
+        x.s = m2 * __ldg(b.lapS + l);
+        const float2 d = __ldg(col + l);
+        x.dr = -d.x;
+        x.di = -d.y;
+#pragma unroll
+        for (int s = 1; s < 32; s <<= 1) {
+            const RowF lo = shfl_row_up(x, s), hi = shfl_row_down(x, s);
+            x = pcr_combine(x, l >= s ? lo : row_bound(), l + s < 32 ? hi : row_bound());
+        }
+        const float inv = rcpf(x.s + x.a + x.c);
+        sol[l] = make_float2(x.dr * inv, x.di * inv);
+    } else {
+        {
+            float2 d[P];
+#pragma unroll
+            for (int q = 0; q < P; q++) d[q] = __ldg(col + q * 32 + l);
+#pragma unroll
+            for (int q = 0; q < P; q++) {
+                const int r = q * 32 + l;
+                cs[r + r / P] = d[q];
+            }
+        }
+        __syncwarp();
+        const int f = l * P;
+        float A[P], C[P], S[P], Dr[P], Di[P];
+        if constexpr (P >= 4) {
+#pragma unroll
+            for (int q = 0; q < P; q += 4) {  // 16-byte aligned quads of table entries
+                const float4 a = ldg4(b.lapA + f + q), c = ldg4(b.lapC + f + q), s = ldg4(b.lapS + f + q);
+                A[q] = a.x, A[q + 1] = a.y, A[q + 2] = a.z, A[q + 3] = a.w;
+                C[q] = c.x, C[q + 1] = c.y, C[q + 2] = c.z, C[q + 3] = c.w;
+                S[q] = m2 * s.x, S[q + 1] = m2 * s.y, S[q + 2] = m2 * s.z, S[q + 3] = m2 * s.w;
+            }
+        } else {
+            const float2 a = ldg2(b.lapA + f), c = ldg2(b.lapC + f), s = ldg2(b.lapS + f);
+            A[0] = a.x, A[1] = a.y;
+            C[0] = c.x, C[1] = c.y;
+            S[0] = m2 * s.x, S[1] = m2 * s.y;
+        }
+#pragma unroll
+        for (int q = 0; q < P; q++) {
+            const float2 d = cs[f + q + l];  // slot of row f + q
+            Dr[q] = -d.x;
+            Di[q] = -d.y;
+        }
+        // downward: rows q >= 2 couple x_f instead of x_{q-1}
+#pragma unroll
+        for (int q = 2; q < P; q++) {
+            float r = A[q] * rcpf(S[q - 1] + A[q - 1] + C[q - 1]);
+            A[q] = r * A[q - 1];
+            S[q] += r * S[q - 1];
+            Dr[q] += r * Dr[q - 1];
+            Di[q] += r * Di[q - 1];
+        }
+        RowF L;
+        L.a = A[P - 1];
+        L.c = C[P - 1];
+        L.s = S[P - 1];
+        L.dr = Dr[P - 1];
+        L.di = Di[P - 1];
+        // upward: rows P-3 .. 1 couple x_f and x_l
+#pragma unroll
+        for (int q = P - 3; q >= 1; q--) {
+            float r = C[q] * rcpf(S[q + 1] + A[q + 1] + C[q + 1]);
+            A[q] += r * A[q + 1];
+            C[q] = r * C[q + 1];
+            S[q] += r * S[q + 1];
+            Dr[q] += r * Dr[q + 1];
+            Di[q] += r * Di[q + 1];
+        }
+        RowF F;
+        F.a = A[0];
+        F.c = C[0];
+        F.s = S[0];
+        F.dr = Dr[0];
+        F.di = Di[0];
+        if (P >= 3) {
+            float r = C[0] * rcpf(S[1] + A[1] + C[1]);
+            F.c = r * C[1];
+            F.s += r * S[1];
+            F.dr += r * Dr[1];
+            F.di += r * Di[1];
+        }
+        // cyclic reduction of the boundary rows 2l (F) and 2l + 1 (L)
+#pragma unroll
+        for (int s = 1; s < 64; s <<= 1) {
+            RowF lf, hf, ll, hl;
+            if (s == 1) {
+                const RowF pL = shfl_row_up(L, 1), nF = shfl_row_down(F, 1);
+                lf = l > 0 ? pL : row_bound();
+                hf = L;
+                ll = F;
+                hl = l < 31 ? nF : row_bound();
+            } else {
+                const int dd = s >> 1;
+                const RowF pF = shfl_row_up(F, dd), pL = shfl_row_up(L, dd);
+                const RowF nF = shfl_row_down(F, dd), nL = shfl_row_down(L, dd);
+                const bool lo = l >= dd, hi = l + dd < 32;
+                lf = lo ? pF : row_bound();
+                ll = lo ? pL : row_bound();
+                hf = hi ? nF : row_bound();
+                hl = hi ? nL : row_bound();
+            }
+            const RowF nF2 = pcr_combine(F, lf, hf), nL2 = pcr_combine(L, ll, hl);
+            F = nF2;
+            L = nL2;
+        }
+        const float iF = rcpf(F.s + F.a + F.c), iL = rcpf(L.s + L.a + L.c);
+        const float xfr = F.dr * iF, xfi = F.di * iF, xlr = L.dr * iL, xli = L.di * iL;
+        cs[f + l] = make_float2(xfr, xfi);
+        cs[f + P - 1 + l] = make_float2(xlr, xli);
+#pragma unroll
+        for (int q = 1; q < P - 1; q++) {
+            float inv = rcpf(S[q] + A[q] + C[q]);
+            cs[f + q + l] =
+                make_float2((Dr[q] + A[q] * xfr + C[q] * xlr) * inv, (Di[q] + A[q] * xfi + C[q] * xli) * inv);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < P; q++) {
+            const int r = q * 32 + l;
+            sol[r] = cs[r + r / P];
+        }
+    }
+}
+
 // FP64 modes: S64 threads (s64_threads: nTheta/2, at most 128) with P =
 // nTheta/threads >= 2 rows each, the same block elimination and boundary-row
 // cyclic reduction as solve_mode32, with every multiplier precomputed in FP64
@@ -987,15 +1158,23 @@ __device__ void solve_mode64(const KGeo& g, const KBufs& b, int m, unsigned char
 }
 
 
-// FP32 rows per thread of the mode solve.
-__host__ __device__ inline int solve_rows(int nt) { return nt >= 256 ? nt / SOLVE_THREADS : 1; }
+// Mode-solve tiles (SOLVE_THREADS threads each).  For nTheta <= 1024 an FP32
+// tile solves SOLVE_THREADS/32 modes, one per warp (solve_warp32); for 2048
+// it solves one mode with the CTA (solve_mode32<16>).  A sphere's tiles:
+// 2 nfp64 FP64 tiles (one right-hand-side component each), then the FP32
+// tiles of modes nfp64 + 1 .. nt.
+__host__ __device__ constexpr int solve_modes_per_tile(int nt) { return nt <= 1024 ? SOLVE_THREADS / 32 : 1; }
+__host__ __device__ inline int solve_tiles(int nt, int nfp64)
+{
+    const int k = solve_modes_per_tile(nt);
+    return 2 * nfp64 + (nt - nfp64 + k - 1) / k;
+}
 
-// Shared memory of one mode solve (FP32 or FP64) of an nt-row sphere.
+// Shared memory of one solve tile (FP32 or FP64) of an nt-row sphere.
 __host__ __device__ inline size_t solve_smem(int nt)
 {
-    const int P = solve_rows(nt);
-    const size_t f32 = P == 1 ? sizeof(float) * 5 * (size_t)nt
-                              : sizeof(float2) * ((size_t)nt + nt / P) + sizeof(float2) * 5 * (size_t)(nt / P);
+    const size_t f32 = nt <= 1024 ? sizeof(float2) * (SOLVE_THREADS / 32) * (size_t)(nt + 32)
+                                  : sizeof(float2) * ((size_t)nt + nt / 16) + sizeof(float2) * 5 * (size_t)(nt / 16);
     const size_t f64 = s64_smem(nt);
     return f32 > f64 ? f32 : f64;
 }
@@ -1017,63 +1196,72 @@ inline size_t solve_smem_max()
     return m;
 }
 
-// Solve tile blk of a sphere (nt + nfp64 tiles): tiles 0 .. 2 nfp64 - 1 are
-// the FP64 modes, one component each (tile 2(m-1) + c: mode m, component
-// c); the rest the FP32 modes nfp64 + 1 .. nt with P rows per thread (P is a
-// runtime value here; the batched kernels mix sizes).
-__device__ __forceinline__ void solve_tile_p(const KGeo& g, const KBufs& b, int nfp64, int blk, int tid,
-                                             unsigned char* smraw, int P)
+// Solve tile blk of an NT-row sphere with nfp64 FP64 modes; every thread of
+// the CTA calls it.  Tile 2(m-1) + c (c = 0, 1): FP64 mode m, component c.
+template <int NT>
+__device__ __forceinline__ void solve_tile_n(const KGeo& g, const KBufs& b, int nfp64, int blk, int tid,
+                                             unsigned char* smraw)
 {
     if (blk < 2 * nfp64) {
-        const int m = (blk >> 1) + 1;
-        const int P64 = g.nt / s64_threads(g.nt);
-        if (blk & 1) {
-            switch (P64) {
-            case 2: solve_mode64<2, 1>(g, b, m, smraw, tid); break;
-            case 4: solve_mode64<4, 1>(g, b, m, smraw, tid); break;
-            case 8: solve_mode64<8, 1>(g, b, m, smraw, tid); break;
-            default: solve_mode64<16, 1>(g, b, m, smraw, tid); break;
-            }
-        } else {
-            switch (P64) {
-            case 2: solve_mode64<2, 0>(g, b, m, smraw, tid); break;
-            case 4: solve_mode64<4, 0>(g, b, m, smraw, tid); break;
-            case 8: solve_mode64<8, 0>(g, b, m, smraw, tid); break;
-            default: solve_mode64<16, 0>(g, b, m, smraw, tid); break;
-            }
-        }
+        constexpr int P64 = NT <= 256 ? 2 : NT / S64_TH;  // NT / s64_threads(NT)
+        if (blk & 1)
+            solve_mode64<P64, 1>(g, b, (blk >> 1) + 1, smraw, tid);
+        else
+            solve_mode64<P64, 0>(g, b, (blk >> 1) + 1, smraw, tid);
         return;
     }
-    const int m = blk - nfp64 + 1;
-    switch (P) {
-    case 1: solve_mode32<1>(g, b, m, smraw, tid); break;
-    case 2: solve_mode32<2>(g, b, m, smraw, tid); break;
-    case 4: solve_mode32<4>(g, b, m, smraw, tid); break;
-    case 8: solve_mode32<8>(g, b, m, smraw, tid); break;
-    default: solve_mode32<16>(g, b, m, smraw, tid); break;
+    if constexpr (NT <= 1024) {
+        const int w = tid >> 5, m = nfp64 + 1 + (blk - 2 * nfp64) * (SOLVE_THREADS / 32) + w;
+        if (w < SOLVE_THREADS / 32 && m <= NT)
+            solve_warp32<NT / 32>(g, b, m, reinterpret_cast<float2*>(smraw) + w * (NT + 32), tid & 31);
+    } else {
+        solve_mode32<NT / SOLVE_THREADS>(g, b, nfp64 + 1 + (blk - 2 * nfp64), smraw, tid);
     }
 }
 
-// All mode solves of a step in one launch: CTAs 0 .. 2 nfp64 - 1 take the
-// FP64 modes, one component of the right-hand side each (CTA 2(m-1) + c:
-// mode m, component c), the rest the FP32 modes nfp64 + 1 .. nt.
-template <int P>
-__global__ void __launch_bounds__(SOLVE_THREADS, 8) k_solve(KGeo g, KBufs b, int nfp64)
+// Runtime dispatch on nTheta (the batched kernels mix sizes).
+__device__ __forceinline__ void solve_tile(const KGeo& g, const KBufs& b, int nfp64, int blk, int tid,
+                                           unsigned char* smraw)
+{
+    switch (g.nt) {
+    case 32: solve_tile_n<32>(g, b, nfp64, blk, tid, smraw); break;
+    case 64: solve_tile_n<64>(g, b, nfp64, blk, tid, smraw); break;
+    case 128: solve_tile_n<128>(g, b, nfp64, blk, tid, smraw); break;
+    case 256: solve_tile_n<256>(g, b, nfp64, blk, tid, smraw); break;
+    case 512: solve_tile_n<512>(g, b, nfp64, blk, tid, smraw); break;
+    case 1024: solve_tile_n<1024>(g, b, nfp64, blk, tid, smraw); break;
+    default: solve_tile_n<2048>(g, b, nfp64, blk, tid, smraw); break;
+    }
+}
+
+// All mode solves of a step in one launch of solve_tiles(NT, nfp64) CTAs of
+// SOLVE_THREADS threads.  Compiled for the residency each size needs: the
+// warp solves of nTheta 512 and 1024 hold 16 and 32 rows per lane in
+// registers (the FP32 tiles of 2048, and the FP64 tiles of every size from
+// 256 up, want more than 64 registers as well).
+__host__ __device__ constexpr int solve_min_ctas(int nt) { return nt == 1024 ? 2 : (nt == 512 ? 3 : (nt >= 256 ? 4 : 8)); }
+template <int NT>
+__global__ void __launch_bounds__(SOLVE_THREADS, solve_min_ctas(NT)) k_solve(KGeo g, KBufs b, int nfp64)
 {
     pdl_wait();
     extern __shared__ __align__(16) unsigned char smraw[];
-    const int blk = blockIdx.x;
-    if (blk < 2 * nfp64) {
-        // FP64 rows per thread: nt / s64_threads(nt), which is P for nt >= 256
-        // and 2 below
-        constexpr int P64 = P < 2 ? 2 : P;
-        if (blk & 1)
-            solve_mode64<P64, 1>(g, b, (blk >> 1) + 1, smraw, threadIdx.x);
-        else
-            solve_mode64<P64, 0>(g, b, (blk >> 1) + 1, smraw, threadIdx.x);
-        return;
+    solve_tile_n<NT>(g, b, nfp64, blockIdx.x, threadIdx.x, smraw);
+}
+
+using SolveKernel = void (*)(KGeo, KBufs, int);
+
+// the instance of k_solve for nTheta = nt
+inline SolveKernel solve_kernel(int nt)
+{
+    switch (nt) {
+    case 32: return k_solve<32>;
+    case 64: return k_solve<64>;
+    case 128: return k_solve<128>;
+    case 256: return k_solve<256>;
+    case 512: return k_solve<512>;
+    case 1024: return k_solve<1024>;
+    default: return k_solve<2048>;
     }
-    solve_mode32<P>(g, b, blk - nfp64 + 1, smraw, threadIdx.x);
 }
 
 // ---------------------------------------------------- inverse FFT + u update

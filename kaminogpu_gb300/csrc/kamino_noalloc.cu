@@ -180,15 +180,12 @@ extern "C" int kamino_projection_noalloc(int n_theta, const float* u_phi, const 
     const int rpc = kk::fft_rows_per_cta(nt);
     const int fft_threads = kk::fft_threads(nt);
     const size_t fft_smem = kk::fft_smem(nt);
-    const int P = kk::solve_rows(nt);
     const size_t solve_smem = kk::solve_smem(nt);
     // same launches as kamino_projection (the divergence from face
     // velocities, the mode solves, the inverse FFT and both gradients)
     kk::div_fft_kernel<2>(nt)<<<nt / rpc, fft_threads, fft_smem, stream>>>(g, b, 0, 1);
-    if (P == 1)
-        kk::k_solve<1><<<nt + NOALLOC_FP64_MODES, nt, solve_smem, stream>>>(g, b, NOALLOC_FP64_MODES);
-    else
-        kk::k_solve<2><<<nt + NOALLOC_FP64_MODES, nt / 2, solve_smem, stream>>>(g, b, NOALLOC_FP64_MODES);
+    kk::solve_kernel(nt)<<<kk::solve_tiles(nt, NOALLOC_FP64_MODES), kk::SOLVE_THREADS, solve_smem, stream>>>(
+        g, b, NOALLOC_FP64_MODES);
     kk::ifft_kernel(nt)<<<nt / rpc, fft_threads, fft_smem, stream>>>(g, b, 0, 1);
     const int nv = kk::elem_groups((nt - 1) * g.np);
     kk::k_vgrad<<<(nv + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS, kk::ELEM_THREADS, 0, stream>>>(g, b, 0, 1);

@@ -456,18 +456,8 @@ static int launch_div(kamino_solver_s* h, int uv_in, int uv_out)
 static int launch_solve(kamino_solver_s* h)
 {
     const KGeo& g = h->g;
-    const int P = kk::solve_rows(g.nt), threads = g.nt / P;
-    void (*k)(KGeo, KBufs, int) = nullptr;
-    switch (P) {
-    case 1: k = kk::k_solve<1>; break;
-    case 2: k = kk::k_solve<2>; break;
-    case 4: k = kk::k_solve<4>; break;
-    case 8: k = kk::k_solve<8>; break;
-    case 16: k = kk::k_solve<16>; break;
-    default: return kamino_fail(KAMINO_ERR_INVALID, "no mode solve for %d rows per thread", P);
-    }
-    // grid: two CTAs per FP64 mode, one per FP32 mode
-    cudaError_t e = kk::launch_pdl(k, g.nt + h->nfp64, threads, h->smem_solve, h->stream, g, h->b, h->nfp64);
+    cudaError_t e = kk::launch_pdl(kk::solve_kernel(g.nt), kk::solve_tiles(g.nt, h->nfp64), kk::SOLVE_THREADS,
+                                   h->smem_solve, h->stream, g, h->b, h->nfp64);
     return launched("k_solve", e);
 }
 
