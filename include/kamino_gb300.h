@@ -319,8 +319,11 @@ int kamino_server_destroy(kamino_server s);
 int kamino_server_submit(kamino_server s, const kamino_config* cfg, const float* u_phi,
                          const float* u_theta, const float* thickness, int32_t steps,
                          double arrival_time_s, int64_t* request_id);
-/* Run one scheduling round: admit queued requests that fit, advance every
- * resident sphere, retire finished ones. */
+/* One pass of the request loop; never waits for the GPU: retires requests
+ * whose work has finished (event queries), admits queued requests that fit
+ * (a large one starts its steps on its own stream), and launches the next
+ * round of the batched spheres if none is in flight.  n_completed: requests
+ * retired by this call.  Call it repeatedly until the work is done. */
 int kamino_server_poll(kamino_server s, int* n_completed);
 /* Copy a finished request's field to host memory (dense pitch) and, for
  * the last field, release it.  KAMINO_ERR_NOT_READY while it runs. */
