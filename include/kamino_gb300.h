@@ -294,11 +294,12 @@ typedef struct kamino_server_config {
                                  stream, concurrently with everything else
                                  (0 = 512); smaller ones advance together in
                                  the batched step                            */
-    int32_t solo_slots;       /* solo requests running at once (0 = 2): each
-                                 large sphere's working set is a good part
-                                 of the L2, and too many at once evict each
-                                 other; a solo request waiting for a slot
-                                 does not hold back smaller ones             */
+    int32_t solo_slots;       /* solo requests running at once (0 = 3): a few
+                                 large spheres together fill the SMs that
+                                 one leaves idle in its latency-bound
+                                 kernels; more evict each other from the L2.
+                                 A solo request waiting for a slot does not
+                                 hold back smaller ones                      */
     int32_t reserved[3];
 } kamino_server_config;
 

@@ -81,9 +81,13 @@ class Batch:
 class Server:
     """Continuous batching of simulate requests under an HBM budget."""
 
-    def __init__(self, budget_bytes, max_resident=0, steps_per_round=10, device=0):
+    def __init__(self, budget_bytes, max_resident=0, steps_per_round=10, device=0, solo_n_theta=0, solo_slots=0):
+        """solo_n_theta: requests with n_theta >= this run as one-sphere graphs
+        on their own streams (0: the library default, 512); solo_slots: how
+        many of those run at once (0: the default, 3)."""
         c = KaminoServerConfig()
         c.budget_bytes, c.max_resident, c.steps_per_round, c.device = budget_bytes, max_resident, steps_per_round, device
+        c.solo_n_theta, c.solo_slots = solo_n_theta, solo_slots
         h = ctypes.c_void_p()
         check(lib.kamino_server_create(ctypes.byref(c), ctypes.byref(h)))
         self._h = h

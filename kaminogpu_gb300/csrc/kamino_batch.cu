@@ -662,7 +662,7 @@ struct kamino_server_s {
         if (round_done) cudaEventDestroy(round_done);
     }
     int solo_n_theta() const { return cfg.solo_n_theta > 0 ? cfg.solo_n_theta : 512; }
-    int solo_slots() const { return cfg.solo_slots > 0 ? cfg.solo_slots : 2; }
+    int solo_slots() const { return cfg.solo_slots > 0 ? cfg.solo_slots : 3; }
     int solo_running() const
     {
         int n = 0;
