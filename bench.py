@@ -11,8 +11,9 @@ value: device time of K steps (CUDA events on the solver's stream; a 256 MiB
   buffer written and then read between steps, so each step starts from a cold
   and clean L2; the state is 25 MB and would otherwise sit in the 129 MB L2).
 e2e:   the same steps through the public C ABI with host buffers: every step
-  copies u_phi, u_theta, thickness in from pinned host memory, steps, and
-  copies them back.
+  is one kamino_step_host call, which copies u_phi, u_theta, thickness in
+  from pinned host memory, steps, and copies them back (the thickness
+  download overlapping the projection).
 --impl reference: the reference has no CPU implementation of this path, so
   the reference arm times the CPU port of its step (oracle/, FP64, all host
   threads) on the same configuration, plus the reference's own CUDA kernels
@@ -184,20 +185,15 @@ def run_ours(args, ws, rank, local, dist):
         ctypes.memmove(p, src[f].ctypes.data, nbytes[f])
     h = s._h
     pitch = 2 * NT * 4
+    io = [bufs[kg.U_PHI], bufs[kg.U_THETA], bufs[kg.THICKNESS]]
     for _ in range(2):  # warm-up of the copy path
-        for f, p in bufs.items():
-            kg.check(L.kamino_set_state(h, f, p, pitch))
-        kg.check(L.kamino_step(h, DT))
-        for f, p in bufs.items():
-            kg.check(L.kamino_get_state(h, f, p, pitch))
+        kg.check(L.kamino_step_host(h, DT, *io, *io, pitch))
     barrier(dist)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        for f, p in bufs.items():
-            kg.check(L.kamino_set_state(h, f, p, pitch))
-        kg.check(L.kamino_step(h, DT))
-        for f, p in bufs.items():
-            kg.check(L.kamino_get_state(h, f, p, pitch))
+        # upload, step and download in one C-ABI call (the same bits as
+        # kamino_set_state x3, kamino_step, kamino_get_state x3)
+        kg.check(L.kamino_step_host(h, DT, *io, *io, pitch))
     e2e_s = time.perf_counter() - t0
     barrier(dist)
     e2e_max = max_over_ranks(dist, e2e_s)

@@ -147,6 +147,18 @@ int kamino_destroy(kamino_handle h);
 int kamino_set_state(kamino_handle h, int field, const float* host, size_t pitch_bytes);
 int kamino_get_state(kamino_handle h, int field, float* host, size_t pitch_bytes);
 
+/* One step with the state in host memory: KaminoQuantity::copyToGPU of
+ * u_phi, u_theta and the thickness, KaminoSolver::stepForward(dt) and
+ * copyBackToCPU of the three (KaminoQuantity.cu:3-18, KaminoSolver.cu:
+ * 197-221) in one call, which returns when the outputs are in host memory.
+ * The thickness download starts as soon as the advection has written it and
+ * overlaps the rest of the step.  Same results as the separate calls; the
+ * in and out buffers may be the same.  pitch_bytes: host row pitch (0 =
+ * dense); pinned host memory (kamino_host_alloc) copies fastest. */
+int kamino_step_host(kamino_handle h, float dt, const float* u_phi_in, const float* u_theta_in,
+                     const float* thickness_in, float* u_phi_out, float* u_theta_out, float* thickness_out,
+                     size_t pitch_bytes);
+
 /* Same, with a device pointer (row pitch in bytes), ordered on the handle's
  * stream and not synchronised. */
 int kamino_set_state_device(kamino_handle h, int field, const float* dev, size_t pitch_bytes);

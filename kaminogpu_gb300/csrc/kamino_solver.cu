@@ -58,6 +58,8 @@ struct kamino_solver_s {
     void* flush = nullptr;
     size_t flush_bytes = 0;
     size_t smem_div = 0, smem_solve = 0, smem_ifft = 0;
+    cudaStream_t io_stream = nullptr;  // kamino_step_host: the early thickness download
+    cudaEvent_t ev_adv = nullptr;      // kamino_step_host: the advection has written its fields
 };
 
 static const char* const kKernelNames[] = {"k_advect", "k_geo_centers", "k_div_fft",
@@ -142,6 +144,9 @@ extern "C" int kamino_destroy(kamino_handle h)
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     destroy_graphs(h);
+    if (h->io_stream) cudaStreamSynchronize(h->io_stream);
+    if (h->ev_adv) cudaEventDestroy(h->ev_adv);
+    if (h->io_stream) cudaStreamDestroy(h->io_stream);
     if (h->arena) cudaFree(h->arena);
     if (h->flush) cudaFree(h->flush);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -476,7 +481,10 @@ static int launch_ifft(kamino_solver_s* h, int uv_in, int uv_out)
 
 // The fused step from parity (cu, cr); ev, when given, receives an external
 // event record before the first and after every kernel (kNumKernels + 1).
-static int enqueue_step(kamino_solver_s* h, int cu, int cr, cudaEvent_t* ev)
+// The six launches of one step from buffer parity (cu, cr).  ev: optional
+// per-kernel timing events (graph capture); after_advect: optional event
+// recorded once the advection has written the step's thickness.
+static int enqueue_step(kamino_solver_s* h, int cu, int cr, cudaEvent_t* ev, cudaEvent_t after_advect = nullptr)
 {
     cudaError_t pending = cudaGetLastError();
     if (pending != cudaSuccess)
@@ -487,6 +495,7 @@ static int enqueue_step(kamino_solver_s* h, int cu, int cr, cudaEvent_t* ev)
     };
     mark(0);
     if (!rc) rc = launch_advect(h, cu, 1 - cu, cr, 1 - cr);
+    if (!rc && after_advect) KCUDA(cudaEventRecord(after_advect, h->stream));
     mark(1);
     if (!rc) rc = launch_geo(h, 1 - cu);
     mark(2);
@@ -848,6 +857,54 @@ extern "C" int kamino_set_state(kamino_handle h, int field, const float* host, s
 extern "C" int kamino_get_state(kamino_handle h, int field, float* host, size_t pitch_bytes)
 {
     return copy_field(h, field, host, pitch_bytes, false, cudaMemcpyDeviceToHost, true);
+}
+
+// One step with the state in host memory (KaminoQuantity::copyToGPU,
+// KaminoSolver::stepForward, KaminoQuantity::copyBackToCPU in one call:
+// KaminoQuantity.cu:3-18, KaminoSolver.cu:197-221).  The thickness is final
+// once the advection has run, so its download starts then, on a second
+// stream, and overlaps the projection; u_phi and u_theta follow the step.
+extern "C" int kamino_step_host(kamino_handle h, float dt, const float* u_phi_in, const float* u_theta_in,
+                                const float* thickness_in, float* u_phi_out, float* u_theta_out,
+                                float* thickness_out, size_t pitch_bytes)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!u_phi_in || !u_theta_in || !thickness_in || !u_phi_out || !u_theta_out || !thickness_out)
+        return kamino_fail(KAMINO_ERR_INVALID, "kamino_step_host: null buffer");
+    const size_t w = sizeof(float) * h->g.np;
+    if (pitch_bytes == 0) pitch_bytes = w;
+    if (pitch_bytes < w) return kamino_fail(KAMINO_ERR_INVALID, "pitch %zu < row bytes %zu", pitch_bytes, w);
+    if (!h->io_stream) {
+        KCUDA(cudaStreamCreateWithFlags(&h->io_stream, cudaStreamNonBlocking));
+        KCUDA(cudaEventCreateWithFlags(&h->ev_adv, cudaEventDisableTiming));
+    }
+    h->last_dt = dt;
+    if ((rc = apply_dt(h, dt))) return rc;
+    if ((rc = copy_field(h, KAMINO_U_PHI, (void*)u_phi_in, pitch_bytes, true, cudaMemcpyHostToDevice, false)) ||
+        (rc = copy_field(h, KAMINO_U_THETA, (void*)u_theta_in, pitch_bytes, true, cudaMemcpyHostToDevice, false)) ||
+        (rc = copy_field(h, KAMINO_THICKNESS, (void*)thickness_in, pitch_bytes, true, cudaMemcpyHostToDevice,
+                         false)))
+        return rc;
+    const int cu = h->cur_uv, cr = h->cur_r;
+    if ((rc = enqueue_step(h, cu, cr, nullptr, h->ev_adv))) return rc;
+    h->cur_uv ^= 1;
+    h->cur_r ^= 1;
+    h->steps++;
+    h->time += h->g.dt;
+    const int rows = h->g.nt;
+    KCUDA(cudaStreamWaitEvent(h->io_stream, h->ev_adv, 0));
+    if (pitch_bytes == w)
+        KCUDA(cudaMemcpyAsync(thickness_out, h->b.rho[h->cur_r], w * rows, cudaMemcpyDeviceToHost, h->io_stream));
+    else
+        KCUDA(cudaMemcpy2DAsync(thickness_out, pitch_bytes, h->b.rho[h->cur_r], w, w, rows, cudaMemcpyDeviceToHost,
+                                h->io_stream));
+    if ((rc = copy_field(h, KAMINO_U_PHI, u_phi_out, pitch_bytes, false, cudaMemcpyDeviceToHost, false)) ||
+        (rc = copy_field(h, KAMINO_U_THETA, u_theta_out, pitch_bytes, false, cudaMemcpyDeviceToHost, false)))
+        return rc;
+    KCUDA(cudaStreamSynchronize(h->io_stream));
+    KCUDA(cudaStreamSynchronize(h->stream));
+    return KAMINO_OK;
 }
 
 extern "C" int kamino_set_state_device(kamino_handle h, int field, const float* dev, size_t pitch_bytes)

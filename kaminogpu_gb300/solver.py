@@ -142,6 +142,18 @@ class KaminoSolver:
     def stepForward(self, dt=None):
         check(lib.kamino_step(self._h, self.config.dt if dt is None else dt))
 
+    def step_host(self, u_phi, u_theta, thickness, dt=None):
+        """One step with the state in host memory (kamino_step_host): uploads
+        the three fields, steps, and returns the new three as arrays."""
+        ins = [np.ascontiguousarray(a, dtype=np.float32) for a in (u_phi, u_theta, thickness)]
+        for f, a in zip((U_PHI, U_THETA, THICKNESS), ins):
+            if a.shape != self._shape(f):
+                raise ValueError("field %d expects shape %s, got %s" % (f, self._shape(f), a.shape))
+        outs = [np.empty_like(a) for a in ins]
+        check(lib.kamino_step_host(self._h, self.config.dt if dt is None else dt, *[a.ctypes.data for a in ins],
+                                   *[o.ctypes.data for o in outs], ins[0].strides[0]))
+        return outs
+
     def advection(self):
         check(lib.kamino_advection(self._h))
 

@@ -146,3 +146,22 @@ def test_fp64_mode_solves_agree(kg, orc, fp64_modes):
     s.close()
     for k in ("u_phi", "u_theta"):
         assert orc.rel_l2(got[k], want[k]) <= TOL, (k, orc.rel_l2(got[k], want[k]))
+
+
+@pytest.mark.parametrize("nt", [64, 512])
+def test_step_host_matches_separate_calls_bitwise(kg, orc, nt):
+    """kamino_step_host (upload, step, download in one call, the thickness
+    download overlapping the projection) gives the bits of set_state x3,
+    kamino_step and get_state x3, over several steps."""
+    st = kg.make_initial_state(nt, lmax=8, seed=9)
+    cfg = kg.default_config(n_theta=nt, radius=1.0, dt=0.003)
+    with kg.KaminoSolver(config=cfg) as a, kg.KaminoSolver(config=cfg) as b:
+        u, v, r = st["u_phi"], st["u_theta"], st["thickness"]
+        b.load(st)
+        for _ in range(3):
+            u, v, r = a.step_host(u, v, r)
+            b.stepForward()
+        want = b.fields()
+    assert np.array_equal(u, want["u_phi"])
+    assert np.array_equal(v, want["u_theta"])
+    assert np.array_equal(r, want["thickness"])
