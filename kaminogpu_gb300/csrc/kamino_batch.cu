@@ -100,17 +100,25 @@ __global__ void __launch_bounds__(kk::ELEM_THREADS) kb_geo(const KSphere* __rest
     }
 }
 
-__global__ void __launch_bounds__(kk::FFT_MAX_THREADS) kb_div_fft(const KSphere* __restrict__ sph, const int2* __restrict__ items,
-                                                  int n, int* counter, int uv_in, int uv_out)
+// The FFT and solve stages come in three instances by the batch's largest
+// nTheta (MAXN = 256, 1024, 2048): a batch of small spheres does not run
+// code sized, in registers, for the 2048-row tiles (the 256 class is held
+// to 128 registers: four CTAs per SM).
+constexpr int fft_stage_min_ctas(int maxn) { return maxn <= 256 ? 4 : 1; }
+template <int MAXN>
+__global__ void __launch_bounds__(kk::FFT_MAX_THREADS, fft_stage_min_ctas(MAXN)) kb_div_fft(const KSphere* __restrict__ sph,
+                                                                  const int2* __restrict__ items, int n,
+                                                                  int* counter, int uv_in, int uv_out)
 {
     extern __shared__ float2 sm2[];
     __shared__ KSphere s;
     __shared__ int s_item;
     int2 w;
     while (next_item(counter, n, items, sph, 1, &s, &s_item, &w))
-        kk::div_fft_tile<0>(s.g, s.b, uv_in, uv_out, w.y, threadIdx.x, sm2);
+        kk::div_fft_tile<0, MAXN>(s.g, s.b, uv_in, uv_out, w.y, threadIdx.x, sm2);
 }
 
+template <int MAXN>
 __global__ void __launch_bounds__(kk::SOLVE_THREADS) kb_solve(const KSphere* __restrict__ sph,
                                                                const int2* __restrict__ items, int n, int* counter)
 {
@@ -119,18 +127,38 @@ __global__ void __launch_bounds__(kk::SOLVE_THREADS) kb_solve(const KSphere* __r
     __shared__ int s_item;
     int2 w;
     while (next_item(counter, n, items, sph, 1, &s, &s_item, &w))
-        kk::solve_tile(s.g, s.b, s.nfp64, w.y, threadIdx.x, smraw);
+        kk::solve_tile<MAXN>(s.g, s.b, s.nfp64, w.y, threadIdx.x, smraw);
 }
 
-__global__ void __launch_bounds__(kk::FFT_MAX_THREADS) kb_ifft(const KSphere* __restrict__ sph, const int2* __restrict__ items,
-                                               int n, int* counter, int uv_in, int uv_out)
+template <int MAXN>
+__global__ void __launch_bounds__(kk::FFT_MAX_THREADS, fft_stage_min_ctas(MAXN)) kb_ifft(const KSphere* __restrict__ sph,
+                                                               const int2* __restrict__ items, int n, int* counter,
+                                                               int uv_in, int uv_out)
 {
     extern __shared__ float2 sm2[];
     __shared__ KSphere s;
     __shared__ int s_item;
     int2 w;
     while (next_item(counter, n, items, sph, 1, &s, &s_item, &w))
-        kk::ifft_tile(s.g, s.b, uv_in, uv_out, w.y, threadIdx.x, sm2);
+        kk::ifft_tile<MAXN>(s.g, s.b, uv_in, uv_out, w.y, threadIdx.x, sm2);
+}
+
+using FftStageKernel = void (*)(const KSphere*, const int2*, int, int*, int, int);
+using SolveStageKernel = void (*)(const KSphere*, const int2*, int, int*);
+
+// smallest size class (256, 1024, 2048) holding nTheta = nt
+inline int size_class(int nt) { return nt <= 256 ? 256 : (nt <= 1024 ? 1024 : 2048); }
+inline FftStageKernel div_stage(int cls)
+{
+    return cls == 256 ? kb_div_fft<256> : (cls == 1024 ? kb_div_fft<1024> : kb_div_fft<2048>);
+}
+inline FftStageKernel ifft_stage(int cls)
+{
+    return cls == 256 ? kb_ifft<256> : (cls == 1024 ? kb_ifft<1024> : kb_ifft<2048>);
+}
+inline SolveStageKernel solve_stage(int cls)
+{
+    return cls == 256 ? kb_solve<256> : (cls == 1024 ? kb_solve<1024> : kb_solve<2048>);
 }
 
 __global__ void __launch_bounds__(kk::ELEM_THREADS) kb_vgrad(const KSphere* __restrict__ sph,
@@ -173,6 +201,7 @@ struct Engine {
     size_t smem_fft = 0, smem_solve = 0;
     int fft_block = 128;  // threads of the FFT kernels: the largest sphere's fft_threads
     int fft_resident = 1; // FFT CTAs of that size resident per SM (registers, shared memory)
+    int cls = 2048;       // size class of the FFT and solve kernels: the largest sphere's
     Shapes shapes;
     int cu = 0, cr = 0;
     cudaGraphExec_t graph[2][2] = {};
@@ -290,19 +319,26 @@ struct Engine {
         smem_fft = 0;
         smem_solve = 0;
         fft_block = 32;
+        int max_nt = 32;
         for (const KSphere& s : host_desc) {
             const int nt = s.g.nt;
             smem_fft = std::max(smem_fft, kk::fft_smem(nt));
             smem_solve = std::max(smem_solve, kk::solve_smem(nt));
             fft_block = std::max(fft_block, kk::fft_threads(nt));
+            max_nt = std::max(max_nt, nt);
         }
-        BCUDA(cudaFuncSetAttribute(kb_div_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kk::fft_smem_max()));
-        BCUDA(cudaFuncSetAttribute(kb_ifft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kk::fft_smem_max()));
-        BCUDA(cudaFuncSetAttribute(kb_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)kk::solve_smem_max()));
+        cls = size_class(max_nt);
+        for (int c : {256, 1024, 2048}) {  // attributes belong to the functions, shared by every engine
+            BCUDA(cudaFuncSetAttribute(div_stage(c), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kk::fft_smem_max()));
+            BCUDA(cudaFuncSetAttribute(ifft_stage(c), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kk::fft_smem_max()));
+            BCUDA(cudaFuncSetAttribute(solve_stage(c), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kk::solve_smem_max()));
+        }
         int occ_div = 1, occ_ifft = 1;
-        BCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_div, kb_div_fft, fft_block, smem_fft));
-        BCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ifft, kb_ifft, fft_block, smem_fft));
+        BCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_div, div_stage(cls), fft_block, smem_fft));
+        BCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ifft, ifft_stage(cls), fft_block, smem_fft));
         fft_resident = std::max(1, std::min(occ_div, occ_ifft));
         BCUDA(cudaStreamSynchronize(stream));  // host tables go out of scope
         return KAMINO_OK;
@@ -328,12 +364,13 @@ struct Engine {
                                                                  n_items[ST_ADV], d_counters + ST_ADV, c, r, tpi);
         kb_geo<<<grid(ST_GEO), kk::ELEM_THREADS, 0, stream>>>(d_desc, d_items + item_off[ST_GEO], n_items[ST_GEO],
                                                                d_counters + ST_GEO, 1 - c, tpi);
-        kb_div_fft<<<grid(ST_DIV), fft_block, smem_fft, stream>>>(d_desc, d_items + item_off[ST_DIV], n_items[ST_DIV],
-                                                            d_counters + ST_DIV, 1 - c, c);
-        kb_solve<<<grid(ST_SOLVE), kk::SOLVE_THREADS, smem_solve, stream>>>(
+        div_stage(cls)<<<grid(ST_DIV), fft_block, smem_fft, stream>>>(d_desc, d_items + item_off[ST_DIV],
+                                                                       n_items[ST_DIV], d_counters + ST_DIV, 1 - c, c);
+        solve_stage(cls)<<<grid(ST_SOLVE), kk::SOLVE_THREADS, smem_solve, stream>>>(
             d_desc, d_items + item_off[ST_SOLVE], n_items[ST_SOLVE], d_counters + ST_SOLVE);
-        kb_ifft<<<grid(ST_IFFT), fft_block, smem_fft, stream>>>(d_desc, d_items + item_off[ST_IFFT], n_items[ST_IFFT],
-                                                          d_counters + ST_IFFT, c, 1 - c);
+        ifft_stage(cls)<<<grid(ST_IFFT), fft_block, smem_fft, stream>>>(d_desc, d_items + item_off[ST_IFFT],
+                                                                        n_items[ST_IFFT], d_counters + ST_IFFT, c,
+                                                                        1 - c);
         kb_vgrad<<<grid(ST_VGRAD), kk::ELEM_THREADS, 0, stream>>>(d_desc, d_items + item_off[ST_VGRAD],
                                                                    n_items[ST_VGRAD], d_counters + ST_VGRAD, c, 1 - c,
                                                                    tpi);

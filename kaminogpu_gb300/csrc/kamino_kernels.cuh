@@ -539,8 +539,10 @@ __device__ __forceinline__ void div_fft_tile_n(const KGeo& g, const KBufs& b, in
     }
 }
 
-// Runtime dispatch on nTheta (the batched kernels mix sizes).
-template <int MODE>
+// Runtime dispatch on nTheta (the batched kernels mix sizes).  MAXN: the
+// largest nTheta the caller can meet; larger sizes are compiled out, so a
+// kernel for batches of small spheres is not sized (registers) for 2048.
+template <int MODE, int MAXN = 2048>
 __device__ __forceinline__ void div_fft_tile(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int blk,
                                              int tid, float2* sm2)
 {
@@ -549,9 +551,15 @@ __device__ __forceinline__ void div_fft_tile(const KGeo& g, const KBufs& b, int 
     case 64: div_fft_tile_n<MODE, 64>(g, b, uv_in, uv_out, blk, tid, sm2); break;
     case 128: div_fft_tile_n<MODE, 128>(g, b, uv_in, uv_out, blk, tid, sm2); break;
     case 256: div_fft_tile_n<MODE, 256>(g, b, uv_in, uv_out, blk, tid, sm2); break;
-    case 512: div_fft_tile_n<MODE, 512>(g, b, uv_in, uv_out, blk, tid, sm2); break;
-    case 1024: div_fft_tile_n<MODE, 1024>(g, b, uv_in, uv_out, blk, tid, sm2); break;
-    default: div_fft_tile_n<MODE, 2048>(g, b, uv_in, uv_out, blk, tid, sm2); break;
+    case 512:
+        if constexpr (MAXN >= 512) div_fft_tile_n<MODE, 512>(g, b, uv_in, uv_out, blk, tid, sm2);
+        break;
+    case 1024:
+        if constexpr (MAXN >= 1024) div_fft_tile_n<MODE, 1024>(g, b, uv_in, uv_out, blk, tid, sm2);
+        break;
+    default:
+        if constexpr (MAXN >= 2048) div_fft_tile_n<MODE, 2048>(g, b, uv_in, uv_out, blk, tid, sm2);
+        break;
     }
 }
 
@@ -1219,7 +1227,9 @@ __device__ __forceinline__ void solve_tile_n(const KGeo& g, const KBufs& b, int 
     }
 }
 
-// Runtime dispatch on nTheta (the batched kernels mix sizes).
+// Runtime dispatch on nTheta (the batched kernels mix sizes), sizes above
+// MAXN compiled out.
+template <int MAXN = 2048>
 __device__ __forceinline__ void solve_tile(const KGeo& g, const KBufs& b, int nfp64, int blk, int tid,
                                            unsigned char* smraw)
 {
@@ -1228,9 +1238,15 @@ __device__ __forceinline__ void solve_tile(const KGeo& g, const KBufs& b, int nf
     case 64: solve_tile_n<64>(g, b, nfp64, blk, tid, smraw); break;
     case 128: solve_tile_n<128>(g, b, nfp64, blk, tid, smraw); break;
     case 256: solve_tile_n<256>(g, b, nfp64, blk, tid, smraw); break;
-    case 512: solve_tile_n<512>(g, b, nfp64, blk, tid, smraw); break;
-    case 1024: solve_tile_n<1024>(g, b, nfp64, blk, tid, smraw); break;
-    default: solve_tile_n<2048>(g, b, nfp64, blk, tid, smraw); break;
+    case 512:
+        if constexpr (MAXN >= 512) solve_tile_n<512>(g, b, nfp64, blk, tid, smraw);
+        break;
+    case 1024:
+        if constexpr (MAXN >= 1024) solve_tile_n<1024>(g, b, nfp64, blk, tid, smraw);
+        break;
+    default:
+        if constexpr (MAXN >= 2048) solve_tile_n<2048>(g, b, nfp64, blk, tid, smraw);
+        break;
     }
 }
 
@@ -1359,6 +1375,8 @@ __device__ __forceinline__ void ifft_tile_n(const KGeo& g, const KBufs& b, int u
     }
 }
 
+// Runtime dispatch on nTheta, sizes above MAXN compiled out.
+template <int MAXN = 2048>
 __device__ __forceinline__ void ifft_tile(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int blk, int tid,
                                           float2* sm2)
 {
@@ -1367,9 +1385,15 @@ __device__ __forceinline__ void ifft_tile(const KGeo& g, const KBufs& b, int uv_
     case 64: ifft_tile_n<64>(g, b, uv_in, uv_out, blk, tid, sm2); break;
     case 128: ifft_tile_n<128>(g, b, uv_in, uv_out, blk, tid, sm2); break;
     case 256: ifft_tile_n<256>(g, b, uv_in, uv_out, blk, tid, sm2); break;
-    case 512: ifft_tile_n<512>(g, b, uv_in, uv_out, blk, tid, sm2); break;
-    case 1024: ifft_tile_n<1024>(g, b, uv_in, uv_out, blk, tid, sm2); break;
-    default: ifft_tile_n<2048>(g, b, uv_in, uv_out, blk, tid, sm2); break;
+    case 512:
+        if constexpr (MAXN >= 512) ifft_tile_n<512>(g, b, uv_in, uv_out, blk, tid, sm2);
+        break;
+    case 1024:
+        if constexpr (MAXN >= 1024) ifft_tile_n<1024>(g, b, uv_in, uv_out, blk, tid, sm2);
+        break;
+    default:
+        if constexpr (MAXN >= 2048) ifft_tile_n<2048>(g, b, uv_in, uv_out, blk, tid, sm2);
+        break;
     }
 }
 
