@@ -165,3 +165,30 @@ def test_step_host_matches_separate_calls_bitwise(kg, orc, nt):
     assert np.array_equal(u, want["u_phi"])
     assert np.array_equal(v, want["u_theta"])
     assert np.array_equal(r, want["thickness"])
+
+
+def test_mid_size_with_particles(kg, orc):
+    """nTheta=512 x nPhi=1024, radius 1, dt=0.002, l<=16, 2^20 particles:
+    fields and particles against the FP64 oracle after 3 steps, then 1000
+    steps keep every particle on the sphere and every field finite."""
+    npart = 1 << 20
+    st, s, o = make_pair(kg, orc, 512, 0.002, lmax=16, npart=npart)
+    s.step_n(3)
+    o.step(3)
+    got, want = s.fields(), o.fields()
+    for k in FIELDS:
+        err = orc.rel_l2(got[k], want[k])
+        assert err <= TOL, "%s after 3 steps (nt=512, 2^20 particles): rel L2 %.3e" % (k, err)
+    gp, wp = got["particles"].astype(np.float64), o.get_state(4)
+    d = np.abs(gp - wp)
+    d[:, 0] = np.minimum(d[:, 0], 2 * np.pi - d[:, 0])
+    assert np.percentile(d, 99.9) < 1e-4, np.percentile(d, 99.9)
+    s.step_n(997)
+    f = s.fields()
+    s.close()
+    for k in FIELDS:
+        assert np.all(np.isfinite(f[k])), k
+    p = f["particles"]
+    assert p.shape == (npart, 2)
+    assert np.all((p[:, 0] >= 0) & (p[:, 0] <= np.float32(2 * np.pi))), "phi out of [0, 2pi]"
+    assert np.all((p[:, 1] >= 0) & (p[:, 1] <= np.pi)), "theta out of [0, pi]"
