@@ -421,6 +421,5 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 }
 
 
-__device__ __forceinline__ int bitrev(int k, int log2n) { return (int)(__brev((unsigned)k) >> (32 - log2n)); }
 
 } // namespace kdev

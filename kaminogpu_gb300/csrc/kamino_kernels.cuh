@@ -644,35 +644,6 @@ __device__ __forceinline__ RowF row_bound()
     return r;
 }
 
-// Shared-memory PCR over R = n rows, one per thread (threads t >= n only
-// synchronise).  sm: 5 n floats, one array per row component.
-__device__ __forceinline__ void pcr_single(RowF& x, float* sm, int n, int t)
-{
-    const bool active = t < n;
-    float *sa = sm, *sc = sm + n, *ss = sm + 2 * n, *sr = sm + 3 * n, *si = sm + 4 * n;
-    auto at = [&](int i) {
-        RowF r;
-        r.a = sa[i];
-        r.c = sc[i];
-        r.s = ss[i];
-        r.dr = sr[i];
-        r.di = si[i];
-        return r;
-    };
-    for (int s = 1; s < n; s <<= 1) {
-        if (active) {
-            sa[t] = x.a;
-            sc[t] = x.c;
-            ss[t] = x.s;
-            sr[t] = x.dr;
-            si[t] = x.di;
-        }
-        __syncthreads();
-        if (active) x = pcr_combine(x, t - s >= 0 ? at(t - s) : row_bound(), t + s < n ? at(t + s) : row_bound());
-        __syncthreads();
-    }
-}
-
 // Shared-memory PCR over the R = 2 TH boundary rows, thread t owning rows
 // 2t (F) and 2t + 1 (L).  sm: 5 TH float2, one (F, L) pair per thread and row
 // component, so consecutive lanes touch consecutive 8-byte slots.
@@ -747,34 +718,16 @@ __device__ __forceinline__ void store_column(float2* __restrict__ col, const flo
     for (int q = t; q < n; q += blockDim.x) col[q] = cs[q + q / P];
 }
 
-// FP32 solve of mode m by one CTA: thread t owns rows [t P, t P + P).  With
-// P == 1 the CTA may be wider than nt (threads t >= nt only synchronise);
-// with P >= 2 it has exactly nt / P threads.
+// FP32 solve of mode m by one CTA of nt / P threads (nTheta = 2048, P = 16):
+// thread t owns rows [t P, t P + P).
 template <int P>
 __device__ void solve_mode32(const KGeo& g, const KBufs& b, int m, unsigned char* smraw, int t)
 {
+    static_assert(P >= 2, "two or more rows per thread");
     const int n = g.nt;
     const float m2 = (float)m * (float)m;
     const float2* __restrict__ col = b.spec + (size_t)(m - 1) * n;
     float2* __restrict__ sol = b.sol + (size_t)(m - 1) * n;
-    if (P == 1) {
-        const bool active = t < n;
-        RowF r;
-        if (active) {
-            r.a = __ldg(b.lapA + t);
-            r.c = __ldg(b.lapC + t);
-            r.s = m2 * __ldg(b.lapS + t);
-            const float2 d = __ldg(col + t);
-            r.dr = -d.x;
-            r.di = -d.y;
-        }
-        pcr_single(r, reinterpret_cast<float*>(smraw), n, t);
-        if (active) {
-            float inv = rcpf(r.s + r.a + r.c);
-            sol[t] = make_float2(r.dr * inv, r.di * inv);
-        }
-        return;
-    }
     const int TH = n / P;
     float2* cs = reinterpret_cast<float2*>(smraw);  // n + n/P slots
     float2* pw = cs + n + TH;                       // 5 TH float2
