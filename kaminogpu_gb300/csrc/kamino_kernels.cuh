@@ -1000,18 +1000,13 @@ __host__ __device__ inline size_t s64_smem(int nt)
 // imaginary part of the right-hand side (the matrix is real, so the two are
 // independent systems: two CTAs on two SMs share the FP64 work of a mode,
 // which on GB300 is bound by the FP64 pipe of the SM), 2 both.
-template <int P, int COMP>
-__device__ void solve_mode64(const KGeo& g, const KBufs& b, int m, unsigned char* smraw, int t)
+template <int P, int COMP, bool HOIST = true>
+__device__ __forceinline__ void solve_mode64(const KGeo& g, const KBufs& b, int m, unsigned char* smraw, int t)
 {
     constexpr int NC = COMP == 2 ? 2 : 1;
     const int n = g.nt, TH = n / P, R = 2 * TH;
     const bool active = t < TH;
     const double* tb = b.s64 + (size_t)(m - 1) * s64_stride(n);
-    {
-        const char* p = reinterpret_cast<const char*>(tb);
-        for (size_t o = (size_t)t * 128; o < sizeof(double) * s64_stride(n); o += (size_t)blockDim.x * 128)
-            asm volatile("prefetch.global.L1 [%0];" ::"l"(p + o));
-    }
     const double *dn = tb, *up = tb + n, *bA = tb + 2 * n, *bC = tb + 3 * n, *bInv = tb + 4 * n;
     const double *rF = tb + 5 * n, *pl = rF + S64_TH, *ph = pl + S64_L * S64_R, *pinv = ph + S64_L * S64_R;
     auto ld = [](const double* p) { return __ldg(p); };
@@ -1019,7 +1014,46 @@ __device__ void solve_mode64(const KGeo& g, const KBufs& b, int m, unsigned char
     float2* __restrict__ sol = b.sol + (size_t)(m - 1) * n;
     float2* cs = reinterpret_cast<float2*>(smraw);          // n + TH slots
     double* xs = reinterpret_cast<double*>(cs + n + TH);    // NC * R: component c at xs + c * R
-    stage_column(cs, col, n, P, t);
+    const int iF = 2 * t, iL = iF + 1;
+    // HOIST: everything this thread reads from global memory is requested up
+    // front, in one round: its share of the spectrum column, and the
+    // reduction's multipliers of its two boundary rows for every level (the
+    // column first: the rest of the table follows it into L1).  Without it
+    // (the batched kernels, whose one function holds every size and would
+    // spill the 32 multipliers) each level reads its multipliers when it
+    // runs; the arithmetic is the same either way.
+    auto prefetch_table = [&]() {
+        const char* p = reinterpret_cast<const char*>(tb);
+        for (size_t o = (size_t)t * 128; o < sizeof(double) * s64_stride(n); o += (size_t)blockDim.x * 128)
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(p + o));
+    };
+    double mul[HOIST ? S64_L : 1][4];  // per level: lower and upper multiplier of row iF, then of row iL
+    if constexpr (HOIST) {
+        float2 stg[P];
+#pragma unroll
+        for (int k = 0; k < P; k++) {
+            const int q = t + k * blockDim.x;
+            if (q < n) stg[k] = __ldg(col + q);
+        }
+#pragma unroll
+        for (int lv = 0; lv < S64_L; lv++) {
+            if ((1 << lv) < R && active) {
+                mul[lv][0] = ld(pl + lv * S64_R + iF);
+                mul[lv][1] = ld(ph + lv * S64_R + iF);
+                mul[lv][2] = ld(pl + lv * S64_R + iL);
+                mul[lv][3] = ld(ph + lv * S64_R + iL);
+            }
+        }
+        prefetch_table();
+#pragma unroll
+        for (int k = 0; k < P; k++) {  // row r at slot r + r/P
+            const int q = t + k * blockDim.x;
+            if (q < n) cs[q + q / P] = stg[k];
+        }
+    } else {
+        prefetch_table();
+        stage_column(cs, col, n, P, t);
+    }
     __syncthreads();
     const int f = t * P;
     double D[NC][P];
@@ -1060,31 +1094,37 @@ __device__ void solve_mode64(const KGeo& g, const KBufs& b, int m, unsigned char
         }
     }
     // cyclic reduction over the R boundary rows: row 2t = F, 2t + 1 = L
-    const int iF = 2 * t, iL = iF + 1;
-    int level = 0;
-    for (int s = 1; s < R; s <<= 1, level++) {
-        if (active) {
 #pragma unroll
-            for (int c = 0; c < NC; c++) {
-                xs[c * R + iF] = F[c];
-                xs[c * R + iL] = L[c];
-            }
-        }
-        __syncthreads();
-        if (active) {
-            const double* L0 = pl + level * S64_R;
-            const double* H0 = ph + level * S64_R;
-            const double aF = ld(L0 + iF), cF = ld(H0 + iF), aL = ld(L0 + iL), cL = ld(H0 + iL);
+    for (int lv = 0; lv < S64_L; lv++) {
+        const int s = 1 << lv;
+        if (s < R) {  // uniform over the CTA
+            if (active) {
 #pragma unroll
-            for (int c = 0; c < NC; c++) {
-                const double* x = xs + c * R;
-                const double lf = iF - s >= 0 ? x[iF - s] : 0.0, hf = iF + s < R ? x[iF + s] : 0.0;
-                const double ll = iL - s >= 0 ? x[iL - s] : 0.0, hl = iL + s < R ? x[iL + s] : 0.0;
-                F[c] = fma(aF, lf, fma(cF, hf, F[c]));
-                L[c] = fma(aL, ll, fma(cL, hl, L[c]));
+                for (int c = 0; c < NC; c++) {
+                    xs[c * R + iF] = F[c];
+                    xs[c * R + iL] = L[c];
+                }
             }
+            __syncthreads();
+            if (active) {
+                double aF, cF, aL, cL;
+                if constexpr (HOIST) {
+                    aF = mul[lv][0], cF = mul[lv][1], aL = mul[lv][2], cL = mul[lv][3];
+                } else {
+                    aF = ld(pl + lv * S64_R + iF), cF = ld(ph + lv * S64_R + iF);
+                    aL = ld(pl + lv * S64_R + iL), cL = ld(ph + lv * S64_R + iL);
+                }
+#pragma unroll
+                for (int c = 0; c < NC; c++) {
+                    const double* x = xs + c * R;
+                    const double lf = iF - s >= 0 ? x[iF - s] : 0.0, hf = iF + s < R ? x[iF + s] : 0.0;
+                    const double ll = iL - s >= 0 ? x[iL - s] : 0.0, hl = iL + s < R ? x[iL + s] : 0.0;
+                    F[c] = fma(aF, lf, fma(cF, hf, F[c]));
+                    L[c] = fma(aL, ll, fma(cL, hl, L[c]));
+                }
+            }
+            __syncthreads();
         }
-        __syncthreads();
     }
     if (NC == 2) {
         if (active) {
@@ -1159,16 +1199,16 @@ inline size_t solve_smem_max()
 
 // Solve tile blk of an NT-row sphere with nfp64 FP64 modes; every thread of
 // the CTA calls it.  Tile 2(m-1) + c (c = 0, 1): FP64 mode m, component c.
-template <int NT>
+template <int NT, bool HOIST = true>
 __device__ __forceinline__ void solve_tile_n(const KGeo& g, const KBufs& b, int nfp64, int blk, int tid,
                                              unsigned char* smraw)
 {
     if (blk < 2 * nfp64) {
         constexpr int P64 = NT <= 256 ? 2 : NT / S64_TH;  // NT / s64_threads(NT)
         if (blk & 1)
-            solve_mode64<P64, 1>(g, b, (blk >> 1) + 1, smraw, tid);
+            solve_mode64<P64, 1, HOIST>(g, b, (blk >> 1) + 1, smraw, tid);
         else
-            solve_mode64<P64, 0>(g, b, (blk >> 1) + 1, smraw, tid);
+            solve_mode64<P64, 0, HOIST>(g, b, (blk >> 1) + 1, smraw, tid);
         return;
     }
     if constexpr (NT <= 1024) {
@@ -1187,18 +1227,18 @@ __device__ __forceinline__ void solve_tile(const KGeo& g, const KBufs& b, int nf
                                            unsigned char* smraw)
 {
     switch (g.nt) {
-    case 32: solve_tile_n<32>(g, b, nfp64, blk, tid, smraw); break;
-    case 64: solve_tile_n<64>(g, b, nfp64, blk, tid, smraw); break;
-    case 128: solve_tile_n<128>(g, b, nfp64, blk, tid, smraw); break;
-    case 256: solve_tile_n<256>(g, b, nfp64, blk, tid, smraw); break;
+    case 32: solve_tile_n<32, false>(g, b, nfp64, blk, tid, smraw); break;
+    case 64: solve_tile_n<64, false>(g, b, nfp64, blk, tid, smraw); break;
+    case 128: solve_tile_n<128, false>(g, b, nfp64, blk, tid, smraw); break;
+    case 256: solve_tile_n<256, false>(g, b, nfp64, blk, tid, smraw); break;
     case 512:
-        if constexpr (MAXN >= 512) solve_tile_n<512>(g, b, nfp64, blk, tid, smraw);
+        if constexpr (MAXN >= 512) solve_tile_n<512, false>(g, b, nfp64, blk, tid, smraw);
         break;
     case 1024:
-        if constexpr (MAXN >= 1024) solve_tile_n<1024>(g, b, nfp64, blk, tid, smraw);
+        if constexpr (MAXN >= 1024) solve_tile_n<1024, false>(g, b, nfp64, blk, tid, smraw);
         break;
     default:
-        if constexpr (MAXN >= 2048) solve_tile_n<2048>(g, b, nfp64, blk, tid, smraw);
+        if constexpr (MAXN >= 2048) solve_tile_n<2048, false>(g, b, nfp64, blk, tid, smraw);
         break;
     }
 }
@@ -1206,9 +1246,9 @@ __device__ __forceinline__ void solve_tile(const KGeo& g, const KBufs& b, int nf
 // All mode solves of a step in one launch of solve_tiles(NT, nfp64) CTAs of
 // SOLVE_THREADS threads.  Compiled for the residency each size needs: the
 // warp solves of nTheta 512 and 1024 hold 16 and 32 rows per lane in
-// registers (the FP32 tiles of 2048, and the FP64 tiles of every size from
-// 256 up, want more than 64 registers as well).
-__host__ __device__ constexpr int solve_min_ctas(int nt) { return nt == 1024 ? 2 : (nt == 512 ? 3 : (nt >= 256 ? 4 : 8)); }
+// registers (the FP32 tiles of 2048, and the FP64 tiles with their reduction
+// multipliers held in registers, want more than 64 as well).
+__host__ __device__ constexpr int solve_min_ctas(int nt) { return nt == 1024 ? 2 : (nt == 512 ? 3 : 4); }
 template <int NT>
 __global__ void __launch_bounds__(SOLVE_THREADS, solve_min_ctas(NT)) k_solve(KGeo g, KBufs b, int nfp64)
 {
