@@ -1028,7 +1028,23 @@ __device__ __forceinline__ void solve_mode64(const KGeo& g, const KBufs& b, int 
             asm volatile("prefetch.global.L1 [%0];" ::"l"(p + o));
     };
     double mul[HOIST ? S64_L : 1][4];  // per level: lower and upper multiplier of row iF, then of row iL
+    constexpr int PH = HOIST ? P : 1;
+    double rdn[PH], rup[PH], ba[PH], bc[PH], bi[PH], rf = 0.0, pF = 0.0, pL = 0.0;  // this thread's rows
     if constexpr (HOIST) {
+        if (active) {
+            const int f0 = t * P;
+#pragma unroll
+            for (int q = 0; q < P; q++) {
+                rdn[q] = q >= 2 ? ld(dn + f0 + q) : 0.0;
+                rup[q] = q >= 1 && q <= P - 3 ? ld(up + f0 + q) : 0.0;
+                ba[q] = q >= 1 && q <= P - 2 ? ld(bA + f0 + q) : 0.0;
+                bc[q] = q >= 1 && q <= P - 2 ? ld(bC + f0 + q) : 0.0;
+                bi[q] = q >= 1 && q <= P - 2 ? ld(bInv + f0 + q) : 0.0;
+            }
+            if (P >= 3) rf = ld(rF + t);
+            pF = ld(pinv + iF);
+            pL = ld(pinv + iL);
+        }
         float2 stg[P];
 #pragma unroll
         for (int k = 0; k < P; k++) {
@@ -1073,7 +1089,7 @@ __device__ __forceinline__ void solve_mode64(const KGeo& g, const KBufs& b, int 
         }
 #pragma unroll
         for (int q = 2; q < P; q++) {
-            const double r = ld(dn + f + q);
+            const double r = HOIST ? rdn[HOIST ? q : 0] : ld(dn + f + q);
 #pragma unroll
             for (int c = 0; c < NC; c++) D[c][q] = fma(r, D[c][q - 1], D[c][q]);
         }
@@ -1081,14 +1097,14 @@ __device__ __forceinline__ void solve_mode64(const KGeo& g, const KBufs& b, int 
         for (int c = 0; c < NC; c++) L[c] = D[c][P - 1];
 #pragma unroll
         for (int q = P - 3; q >= 1; q--) {
-            const double r = ld(up + f + q);
+            const double r = HOIST ? rup[HOIST ? q : 0] : ld(up + f + q);
 #pragma unroll
             for (int c = 0; c < NC; c++) D[c][q] = fma(r, D[c][q + 1], D[c][q]);
         }
 #pragma unroll
         for (int c = 0; c < NC; c++) F[c] = D[c][0];
         if (P >= 3) {
-            const double r = ld(rF + t);
+            const double r = HOIST ? rf : ld(rF + t);
 #pragma unroll
             for (int c = 0; c < NC; c++) F[c] = fma(r, D[c][1], F[c]);
         }
@@ -1147,13 +1163,18 @@ __device__ __forceinline__ void solve_mode64(const KGeo& g, const KBufs& b, int 
     if (!active) return;
     // one component: its float of each solution entry
     float* __restrict__ sc = reinterpret_cast<float*>(sol) + (COMP == 1 ? 1 : 0);
-    const double pF = ld(pinv + iF), pL = ld(pinv + iL);
+    if constexpr (!HOIST) {
+        pF = ld(pinv + iF);
+        pL = ld(pinv + iL);
+    }
     const double xf = F[0] * pF, xl = L[0] * pL;
     sc[2 * f] = (float)xf;
     sc[2 * (f + P - 1)] = (float)xl;
 #pragma unroll
     for (int q = 1; q < P - 1; q++) {
-        const double a = ld(bA + f + q), c = ld(bC + f + q), iv = ld(bInv + f + q);
+        const double a = HOIST ? ba[HOIST ? q : 0] : ld(bA + f + q);
+        const double c = HOIST ? bc[HOIST ? q : 0] : ld(bC + f + q);
+        const double iv = HOIST ? bi[HOIST ? q : 0] : ld(bInv + f + q);
         sc[2 * (f + q)] = (float)(fma(a, xf, fma(c, xl, D[0][q])) * iv);
     }
 }
@@ -1206,9 +1227,9 @@ __device__ __forceinline__ void solve_tile_n(const KGeo& g, const KBufs& b, int 
     if (blk < 2 * nfp64) {
         constexpr int P64 = NT <= 256 ? 2 : NT / S64_TH;  // NT / s64_threads(NT)
         if (blk & 1)
-            solve_mode64<P64, 1, HOIST>(g, b, (blk >> 1) + 1, smraw, tid);
+            solve_mode64<P64, 1, HOIST && NT <= 1024>(g, b, (blk >> 1) + 1, smraw, tid);
         else
-            solve_mode64<P64, 0, HOIST>(g, b, (blk >> 1) + 1, smraw, tid);
+            solve_mode64<P64, 0, HOIST && NT <= 1024>(g, b, (blk >> 1) + 1, smraw, tid);
         return;
     }
     if constexpr (NT <= 1024) {
