@@ -103,8 +103,8 @@ __global__ void __launch_bounds__(kk::ELEM_THREADS) kb_geo(const KSphere* __rest
 // The FFT and solve stages come in three instances by the batch's largest
 // nTheta (MAXN = 256, 1024, 2048): a batch of small spheres does not run
 // code sized, in registers, for the 2048-row tiles (the 256 class is held
-// to 128 registers: four CTAs per SM).
-constexpr int fft_stage_min_ctas(int maxn) { return maxn <= 256 ? 4 : 1; }
+// to 128 registers).
+constexpr int fft_stage_min_ctas(int maxn) { return maxn <= 256 ? 2 : 1; }
 template <int MAXN>
 __global__ void __launch_bounds__(kk::FFT_MAX_THREADS, fft_stage_min_ctas(MAXN)) kb_div_fft(const KSphere* __restrict__ sph,
                                                                   const int2* __restrict__ items, int n,

@@ -292,8 +292,13 @@ __host__ __device__ constexpr int brev(int i, int bits)
 }
 __host__ __device__ constexpr int fft_lanes(int nt) { return 1 << (ilog2c(nt) / 2); }
 __host__ __device__ constexpr int fft_rows_per_cta(int nt) { return fft_lanes(nt) == 4 ? 8 : 4; }
-__host__ __device__ constexpr int fft_threads(int nt) { return fft_rows_per_cta(nt) * fft_lanes(nt); }
-constexpr int FFT_MAX_THREADS = 128;  // fft_threads of every supported nTheta is at most this
+// nTheta = 1024 runs its 4 rows on 8 warps (the tiles *_w8 below)
+__host__ __device__ constexpr bool fft_w8(int nt) { return nt == 1024; }
+__host__ __device__ constexpr int fft_threads(int nt)
+{
+    return fft_w8(nt) ? 2 * fft_rows_per_cta(nt) * fft_lanes(nt) : fft_rows_per_cta(nt) * fft_lanes(nt);
+}
+constexpr int FFT_MAX_THREADS = 256;  // fft_threads of every supported nTheta is at most this
 // Staging of R rows' mode columns: (mode index mi, row r2) at sidx(); the
 // skew mi R/16 puts 16 consecutive modes of one row on distinct bank pairs.
 __host__ __device__ constexpr int fft_stage_len(int nt) { return nt * fft_rows_per_cta(nt) / 16 * 17; }
@@ -307,10 +312,16 @@ __host__ __device__ constexpr int fft_tblock(int nt)
     return (nt / fft_lanes(nt)) * (fft_lanes(nt) + 1) +
            (fft_lanes(nt) >= 16 ? 0 : (24 - ((nt / fft_lanes(nt)) * (fft_lanes(nt) + 1)) % 16) % 16);
 }
+// float2 slots of the transpose/staging region
+__host__ __device__ constexpr int fft_region_len(int nt)
+{
+    return fft_rows_per_cta(nt) * fft_tblock(nt) > fft_stage_len(nt) ? fft_rows_per_cta(nt) * fft_tblock(nt)
+                                                                     : fft_stage_len(nt);
+}
+// plus, for the 8-warp tiles, the CTA's rows between the phases
 __host__ __device__ inline size_t fft_smem(int nt)
 {
-    const int t = fft_rows_per_cta(nt) * fft_tblock(nt), s = fft_stage_len(nt);
-    return sizeof(float2) * (size_t)(t > s ? t : s);
+    return sizeof(float2) * ((size_t)fft_region_len(nt) + (fft_w8(nt) ? (size_t)fft_rows_per_cta(nt) * nt : 0));
 }
 
 // e^{-2 pi i k/64}, k < 32: the twiddles of the in-register transforms
@@ -393,6 +404,143 @@ __device__ __forceinline__ void row_fft(float2* a, float2* tb, int l, const floa
     for (int s = 0; s < S; s++) fft_regs<L, INV>(a + s * L);
 }
 
+// nTheta = 1024: the CTA's 4 rows on 8 warps.  All 8 share the input (the
+// divergence, half a row each), the unpacking (half the modes of a row
+// each) and the spectrum stores; the transform of each row runs on one warp
+// (row_fft) in between, the rows passing through shared memory behind the
+// transpose/staging region.  One warp per row for every phase left the 7 or
+// 8 rows an SM holds latency-bound from end to end.
+template <int MODE>
+__device__ __forceinline__ void div_fft_tile_w8(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int blk,
+                                                int tid, float2* sm2)
+{
+    constexpr int N = 1024, P = 32, R = 4, LGR = 2, np = 2 * N, H = P / 2;
+    const int w = tid >> 5, l = tid & 31, lr = w & 3, h = w >> 2;
+    const int j0 = blk * R, j = j0 + lr;
+    float2* zrow = sm2 + fft_region_len(N) + lr * N;  // this warp's row: z_n, then X_k
+    {
+        // divergence of points n = l + 32 r, r in [16h, 16h + 16)
+        const float* __restrict__ src = MODE == 0 ? b.cu : b.u[uv_in];
+        const float* __restrict__ vf = b.v[uv_in];
+        float* __restrict__ uo = b.u[uv_out];
+        float* __restrict__ vo = b.v[uv_out];
+        const float fct = __ldg(b.divf + j), sN = __ldg(b.sinN + j), sS = __ldg(b.sinS + j);
+        const size_t row = (size_t)j * np;
+        // c[q] holds register r = 16h + q - 1 (mod 32): the half plus one on each side
+        float2 c[H + 2];
+#pragma unroll
+        for (int q = 0; q < H + 2; q++) c[q] = ldg2(src + row + 2 * (l + 32 * ((16 * h + q - 1) & (P - 1))));
+        const int wl = (l - 1) & 31, el = (l + 1) & 31;
+        constexpr int CH = 8;
+        const float2 zero = make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int q0 = 0; q0 < H; q0 += CH) {
+            float2 vA[CH], vB[CH], vC[CH];  // MODE 0: cv rows j-1, j, j+1; MODE 2: vf rows j-1, j
+#pragma unroll
+            for (int qq = 0; qq < CH; qq++) {
+                const int i = 2 * (l + 32 * (16 * h + q0 + qq));
+                if (MODE == 0) {
+                    vB[qq] = ldg2(b.cv + row + i);
+                    vA[qq] = j > 0 ? ldg2(b.cv + row - np + i) : zero;
+                    vC[qq] = j < N - 1 ? ldg2(b.cv + row + np + i) : zero;
+                } else {
+                    vA[qq] = j > 0 ? ldg2(vf + row - np + i) : zero;
+                    vB[qq] = j < N - 1 ? ldg2(vf + row + i) : zero;
+                }
+            }
+#pragma unroll
+            for (int qq = 0; qq < CH; qq++) {
+                const int q = q0 + qq, n = l + 32 * (16 * h + q), i = 2 * n;
+                const float2 cc = c[q + 1];
+                // phi neighbours f_{2n-1}, f_{2n+2}: lane l -+ 1 of this register; for
+                // lane 0 (31) lane 31 (0) of the previous (next) register
+                const float wsh = __shfl_sync(0xffffffffu, cc.y, wl), wpv = __shfl_sync(0xffffffffu, c[q].y, wl);
+                const float esh = __shfl_sync(0xffffffffu, cc.x, el), enx = __shfl_sync(0xffffffffu, c[q + 2].x, el);
+                const float cl = l == 0 ? wpv : wsh, cr = l == 31 ? enx : esh;
+                float uW[2], uE[2], vN[2], vS[2];
+                if (MODE == 0) {
+                    // assignPhiKernel / assignThetaKernel, KaminoCore.cu:531-533, 546-548
+                    uW[0] = 0.5f * __fadd_rn(cl, cc.x);
+                    uE[0] = 0.5f * __fadd_rn(cc.x, cc.y);
+                    uW[1] = uE[0];
+                    uE[1] = 0.5f * __fadd_rn(cc.y, cr);
+                    if (j > 0) {
+                        vN[0] = 0.5f * __fadd_rn(vA[qq].x, vB[qq].x);
+                        vN[1] = 0.5f * __fadd_rn(vA[qq].y, vB[qq].y);
+                    } else {
+                        vN[0] = vN[1] = 0.0f;
+                    }
+                    if (j < N - 1) {
+                        vS[0] = 0.5f * __fadd_rn(vB[qq].x, vC[qq].x);
+                        vS[1] = 0.5f * __fadd_rn(vB[qq].y, vC[qq].y);
+                        *reinterpret_cast<float2*>(vo + row + i) = make_float2(vS[0], vS[1]);
+                    } else {
+                        vS[0] = vS[1] = 0.0f;
+                    }
+                    *reinterpret_cast<float2*>(uo + row + i) = make_float2(uW[0], uW[1]);
+                } else {
+                    uW[0] = cc.x;
+                    uE[0] = cc.y;
+                    uW[1] = cc.y;
+                    uE[1] = cr;
+                    vN[0] = vA[qq].x;
+                    vN[1] = vA[qq].y;
+                    vS[0] = vB[qq].x;
+                    vS[1] = vB[qq].y;
+                }
+                float d[2];
+#pragma unroll
+                for (int e = 0; e < 2; e++) {
+                    // fillDivergenceKernel, KaminoCore.cu:625-632
+                    float termTheta = __fmul_rn(fct, __fsub_rn(__fmul_rn(vS[e], sS), __fmul_rn(vN[e], sN)));
+                    float termPhi = __fmul_rn(fct, __fsub_rn(uE[e], uW[e]));
+                    d[e] = __fadd_rn(termTheta, termPhi);
+                }
+                zrow[n] = make_float2(d[0], d[1]);  // z_n = f_{2n} + i f_{2n+1}
+            }
+        }
+    }
+    __syncthreads();
+    if (h == 0) {  // the row's transform on one warp
+        float2 a[P];
+#pragma unroll
+        for (int r = 0; r < P; r++) a[r] = zrow[l + 32 * r];
+        row_fft<N, false>(a, sm2 + lr * fft_tblock(N), l, b.tw);
+#pragma unroll
+        for (int k2 = 0; k2 < 32; k2++) zrow[l + 32 * k2] = a[brev(k2, 5)];  // X_{l + 32 k2}
+    }
+    __syncthreads();  // every transpose block is read before the staging reuses the region
+    {
+        // c_m = (1/nPhi)[E_m + e^{-i pi m/N} O_m], m = l + 32 k2, k2 in [16h, 16h + 16)
+        const float scale = 1.0f / (float)np;
+#pragma unroll
+        for (int q = 0; q < H; q++) {
+            const int m = l + 32 * (16 * h + q);
+            const float2 za = zrow[m];
+            float2 c;
+            int mi;
+            if (m == 0) {  // c_N (real): Re Z_0 - Im Z_0
+                c = make_float2((za.x - za.y) * scale, 0.0f);
+                mi = N - 1;
+            } else {
+                const float2 zb = zrow[N - m];
+                const float2 wa = __ldg(b.rt + m);
+                const float er = 0.5f * (za.x + zb.x), ei = 0.5f * (za.y - zb.y);
+                const float orr = 0.5f * (za.y + zb.y), oi = -0.5f * (za.x - zb.x);
+                c = make_float2((er + wa.x * orr - wa.y * oi) * scale, (ei + wa.x * oi + wa.y * orr) * scale);
+                mi = m - 1;
+            }
+            sm2[sidx<R>(mi, lr)] = c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < N * R / (8 * 32); k++) {
+        const int q = tid + k * (8 * 32), r2 = q & (R - 1), mi = q >> LGR;
+        b.spec[(size_t)mi * N + j0 + r2] = sm2[sidx<R>(mi, r2)];
+    }
+}
+
 // Divergence and forward real FFT of latitude rows.
 // MODE 0: from cell centres, also writing u**, v** (the fused step)
 // MODE 2: from face velocities (projection stage called by itself)
@@ -404,6 +552,10 @@ template <int MODE, int N>
 __device__ __forceinline__ void div_fft_tile_n(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int blk,
                                                int tid, float2* sm2)
 {
+    if constexpr (fft_w8(N)) {
+        if (tid < fft_threads(N)) div_fft_tile_w8<MODE>(g, b, uv_in, uv_out, blk, tid, sm2);
+        return;
+    } else {
     constexpr int L = fft_lanes(N), P = N / L, S = P / L, R = fft_rows_per_cta(N);
     constexpr int LGL = ilog2c(L), LGR = ilog2c(R);
     constexpr int np = 2 * N;
@@ -537,6 +689,7 @@ __device__ __forceinline__ void div_fft_tile_n(const KGeo& g, const KBufs& b, in
         const int r2 = q & (R - 1), mi = q >> LGR;
         b.spec[(size_t)mi * N + j0 + r2] = sm2[sidx<R>(mi, r2)];
     }
+    }
 }
 
 // Runtime dispatch on nTheta (the batched kernels mix sizes).  MAXN: the
@@ -564,7 +717,7 @@ __device__ __forceinline__ void div_fft_tile(const KGeo& g, const KBufs& b, int 
 }
 
 template <int MODE, int N>
-__global__ void __launch_bounds__(fft_threads(N)) k_div_fft(KGeo g, KBufs b, int uv_in, int uv_out)
+__global__ void __launch_bounds__(fft_threads(N), fft_w8(N) ? 2 : 1) k_div_fft(KGeo g, KBufs b, int uv_in, int uv_out)
 {
     pdl_wait();
     extern __shared__ float2 sm2[];
@@ -1303,10 +1456,90 @@ inline SolveKernel solve_kernel(int nt)
 // spectrum, whose output is z_k = p_{2k} + i p_{2k+1}.  The solution is
 // mode-major (sol[(m-1)*nt + row]); the CTA first stages its R rows' columns
 // with the row index fastest.
+// nTheta = 1024 inverse on 8 warps: all 8 stage the solution columns, form
+// Y (half a row each) and update u (half a row each); the transform of each
+// row runs on one warp in between, the rows passing through shared memory.
+__device__ __forceinline__ void ifft_tile_w8(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int blk, int tid,
+                                             float2* sm2)
+{
+    constexpr int N = 1024, P = 32, R = 4, LGR = 2, np = 2 * N, H = P / 2, T = 8 * 32;
+    const int w = tid >> 5, l = tid & 31, lr = w & 3, h = w >> 2;
+    const int j0 = blk * R, j = j0 + lr;
+    float2* zrow = sm2 + fft_region_len(N) + lr * N;  // this warp's row: Y_m, then z_k
+    {
+        float2 t[N * R / T];
+#pragma unroll
+        for (int k = 0; k < N * R / T; k++) {
+            const int q = tid + k * T, r2 = q & (R - 1), mi = q >> LGR;
+            t[k] = __ldg(b.sol + (size_t)mi * N + j0 + r2);
+        }
+#pragma unroll
+        for (int k = 0; k < N * R / T; k++) {
+            const int q = tid + k * T, r2 = q & (R - 1), mi = q >> LGR;
+            sm2[sidx<R>(mi, r2)] = t[k];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < H; q++) {
+        const int m = l + 32 * (16 * h + q);
+        if (m == 0) {
+            const float un = sm2[sidx<R>(N - 1, lr)].x;  // X_nt = U_nt, real
+            zrow[0] = make_float2(un, -un);
+            continue;
+        }
+        // X_m = U_m, and X_{m+nt} = conj(U_{nt-m})
+        const float2 ua = sm2[sidx<R>(m - 1, lr)], ub = sm2[sidx<R>(N - m - 1, lr)];
+        const float2 ea = __ldg(b.rt + m);
+        const float Er = ua.x + ub.x, Ei = ua.y - ub.y, Dr = ua.x - ub.x, Di = ua.y + ub.y;
+        const float Or = Dr * ea.x + Di * ea.y, Oi = Di * ea.x - Dr * ea.y;  // D * e^{+i pi m/nt}
+        zrow[m] = make_float2(Er - Oi, Ei + Or);
+    }
+    __syncthreads();  // the staging is read before the transpose blocks reuse it
+    if (h == 0) {
+        float2 a[P];
+#pragma unroll
+        for (int r = 0; r < P; r++) a[r] = zrow[l + 32 * r];
+        row_fft<N, true>(a, sm2 + lr * fft_tblock(N), l, b.tw);
+#pragma unroll
+        for (int k2 = 0; k2 < 32; k2++) zrow[l + 32 * k2] = a[brev(k2, 5)];  // z_{l + 32 k2}
+    }
+    __syncthreads();
+    const float* __restrict__ uf = b.u[uv_in];
+    float* __restrict__ uo = b.u[uv_out];
+    // applyPressurePhi (KaminoCore.cu:740-746) divides by -h sin(theta_j): here
+    // one reciprocal per row, then products
+    const float inhs = __frcp_rn(__ldg(b.negHs + j));
+    const size_t row = (size_t)j * np;
+    constexpr int CH = 8;  // u loads in flight per lane
+#pragma unroll
+    for (int q0 = 0; q0 < H; q0 += CH) {
+        float2 uu[CH];
+#pragma unroll
+        for (int qq = 0; qq < CH; qq++) uu[qq] = ldg2(uf + row + 2 * (l + 32 * (16 * h + q0 + qq)));
+#pragma unroll
+        for (int qq = 0; qq < CH; qq++) {
+            const int k = l + 32 * (16 * h + q0 + qq);
+            // p_{2k} = zc.x, p_{2k+1} = zc.y; the west neighbour p_{2k-1} = Im z_{k-1}
+            const float2 zc = zrow[k];
+            const float zpy = zrow[(k - 1) & (N - 1)].y;
+            float2 o;
+            o.x = __fadd_rn(uu[qq].x, __fmul_rn(__fsub_rn(zc.x, zpy), inhs));
+            o.y = __fadd_rn(uu[qq].y, __fmul_rn(__fsub_rn(zc.y, zc.x), inhs));
+            *reinterpret_cast<float2*>(uo + row + 2 * k) = o;
+            *reinterpret_cast<float2*>(b.p + row + 2 * k) = zc;
+        }
+    }
+}
+
 template <int N>
 __device__ __forceinline__ void ifft_tile_n(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int blk, int tid,
                                             float2* sm2)
 {
+    if constexpr (fft_w8(N)) {
+        if (tid < fft_threads(N)) ifft_tile_w8(g, b, uv_in, uv_out, blk, tid, sm2);
+        return;
+    } else {
     constexpr int L = fft_lanes(N), P = N / L, S = P / L, R = fft_rows_per_cta(N);
     constexpr int LGL = ilog2c(L), LGR = ilog2c(R);
     constexpr int np = 2 * N;
@@ -1387,6 +1620,7 @@ __device__ __forceinline__ void ifft_tile_n(const KGeo& g, const KBufs& b, int u
             *reinterpret_cast<float2*>(b.p + row + 2 * k) = zc;
         }
     }
+    }
 }
 
 // Runtime dispatch on nTheta, sizes above MAXN compiled out.
@@ -1412,7 +1646,7 @@ __device__ __forceinline__ void ifft_tile(const KGeo& g, const KBufs& b, int uv_
 }
 
 template <int N>
-__global__ void __launch_bounds__(fft_threads(N)) k_ifft_u(KGeo g, KBufs b, int uv_in, int uv_out)
+__global__ void __launch_bounds__(fft_threads(N), fft_w8(N) ? 2 : 1) k_ifft_u(KGeo g, KBufs b, int uv_in, int uv_out)
 {
     pdl_wait();
     extern __shared__ float2 sm2[];
