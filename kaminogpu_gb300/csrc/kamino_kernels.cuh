@@ -1698,10 +1698,32 @@ __device__ __forceinline__ void vgrad_tile(const KGeo& g, const KBufs& b, int uv
     *reinterpret_cast<float4*>(b.v[uv_out] + idx) = o;
 }
 
+// vgrad_tile for two groups q0, q1, all six loads in flight together (the
+// one-sphere kernel: a thread per two groups, a block's groups contiguous)
+__device__ __forceinline__ void vgrad_tile2(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int q0, int q1)
+{
+    const int lim = (g.nt - 1) * g.np, i0 = q0 * ELEM_VEC, i1 = q1 * ELEM_VEC;
+    const bool ok0 = i0 < lim, ok1 = i1 < lim;
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 pn0 = ok0 ? ldg4(b.p + i0) : z, ps0 = ok0 ? ldg4(b.p + i0 + g.np) : z, v0 = ok0 ? ldg4(b.v[uv_in] + i0) : z;
+    const float4 pn1 = ok1 ? ldg4(b.p + i1) : z, ps1 = ok1 ? ldg4(b.p + i1 + g.np) : z, v1 = ok1 ? ldg4(b.v[uv_in] + i1) : z;
+    const float ninv = -g.invh;
+    auto upd = [&](const float4& pn, const float4& ps, const float4& v) {
+        float4 o;
+        o.x = __fadd_rn(v.x, __fmul_rn(__fsub_rn(ps.x, pn.x), ninv));
+        o.y = __fadd_rn(v.y, __fmul_rn(__fsub_rn(ps.y, pn.y), ninv));
+        o.z = __fadd_rn(v.z, __fmul_rn(__fsub_rn(ps.z, pn.z), ninv));
+        o.w = __fadd_rn(v.w, __fmul_rn(__fsub_rn(ps.w, pn.w), ninv));
+        return o;
+    };
+    if (ok0) *reinterpret_cast<float4*>(b.v[uv_out] + i0) = upd(pn0, ps0, v0);
+    if (ok1) *reinterpret_cast<float4*>(b.v[uv_out] + i1) = upd(pn1, ps1, v1);
+}
 __global__ void __launch_bounds__(ELEM_THREADS) k_vgrad(KGeo g, KBufs b, int uv_in, int uv_out)
 {
     pdl_wait();
-    vgrad_tile(g, b, uv_in, uv_out, blockIdx.x * blockDim.x + threadIdx.x);
+    const int q = blockIdx.x * (2 * ELEM_THREADS) + threadIdx.x;
+    vgrad_tile2(g, b, uv_in, uv_out, q, q + ELEM_THREADS);
 }
 
 // ------------------------------------------------------------- L2 flush

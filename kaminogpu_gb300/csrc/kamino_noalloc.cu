@@ -188,7 +188,7 @@ extern "C" int kamino_projection_noalloc(int n_theta, const float* u_phi, const 
         g, b, NOALLOC_FP64_MODES);
     kk::ifft_kernel(nt)<<<nt / rpc, fft_threads, fft_smem, stream>>>(g, b, 0, 1);
     const int nv = kk::elem_groups((nt - 1) * g.np);
-    kk::k_vgrad<<<(nv + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS, kk::ELEM_THREADS, 0, stream>>>(g, b, 0, 1);
+    kk::k_vgrad<<<(nv + 2 * kk::ELEM_THREADS - 1) / (2 * kk::ELEM_THREADS), kk::ELEM_THREADS, 0, stream>>>(g, b, 0, 1);
     e = cudaGetLastError();
     if (e != cudaSuccess)
         return kamino_fail(KAMINO_ERR_CUDA, "kamino_projection_noalloc: launch: %s", cudaGetErrorString(e));

@@ -474,7 +474,7 @@ static int launch_ifft(kamino_solver_s* h, int uv_in, int uv_out)
                                    g, h->b, uv_in, uv_out);
     if (int rc = launched("k_ifft_u", e)) return rc;
     int n = kk::elem_groups((g.nt - 1) * g.np);
-    e = kk::launch_pdl(kk::k_vgrad, (n + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS, kk::ELEM_THREADS, 0, h->stream, g,
+    e = kk::launch_pdl(kk::k_vgrad, (n + 2 * kk::ELEM_THREADS - 1) / (2 * kk::ELEM_THREADS), kk::ELEM_THREADS, 0, h->stream, g,
                        h->b, uv_in, uv_out);
     return launched("k_vgrad", e);
 }
@@ -514,7 +514,7 @@ static int enqueue_step(kamino_solver_s* h, int cu, int cr, cudaEvent_t* ev, cud
     if (!rc) {
         const KGeo& g = h->g;
         int n = kk::elem_groups((g.nt - 1) * g.np);
-        cudaError_t e = kk::launch_pdl(kk::k_vgrad, (n + kk::ELEM_THREADS - 1) / kk::ELEM_THREADS, kk::ELEM_THREADS,
+        cudaError_t e = kk::launch_pdl(kk::k_vgrad, (n + 2 * kk::ELEM_THREADS - 1) / (2 * kk::ELEM_THREADS), kk::ELEM_THREADS,
                                        0, h->stream, g, h->b, cu, 1 - cu);
         rc = launched("k_vgrad", e);
     }
