@@ -282,7 +282,8 @@ __device__ __forceinline__ float2 shfl2(float2 v, int src, int width)
 // spectrum and solution columns it exchanges with global memory are whole
 // 32-byte sectors (R rows x 8 bytes), staged in shared memory with the row
 // index fastest.  The transpose blocks and the staging area share the
-// dynamic shared memory; a CTA barrier separates their uses.
+// dynamic shared memory; a CTA barrier separates their uses.  At N = 1024
+// the CTA has twice the warps its rows' transforms need (the *_w8 tiles).
 __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n >> 1); }
 __host__ __device__ constexpr int brev(int i, int bits)
 {
