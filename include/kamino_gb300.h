@@ -147,6 +147,13 @@ int kamino_destroy(kamino_handle h);
 int kamino_set_state(kamino_handle h, int field, const float* host, size_t pitch_bytes);
 int kamino_get_state(kamino_handle h, int field, float* host, size_t pitch_bytes);
 
+/* Replaces KaminoSolver::initialize_velocity (KaminoInitializer.cu:3-85),
+ * which the reference's constructor runs (KaminoSolver.cu:59): sets u_phi
+ * and u_theta to the reference's FBM curl-noise velocity, evaluated on the
+ * device with the reference's float/double arithmetic.  kamino_create
+ * leaves every field zero; call this for the reference's default start. */
+int kamino_init_fbm(kamino_handle h);
+
 /* One step with the state in host memory: KaminoQuantity::copyToGPU of
  * u_phi, u_theta and the thickness, KaminoSolver::stepForward(dt) and
  * copyBackToCPU of the three (KaminoQuantity.cu:3-18, KaminoSolver.cu:

@@ -117,6 +117,7 @@ SIGNATURES = {
     "kamino_get_state_device": (_I, [_P, _I, _P, _SZ]),
     "kamino_step": (_I, [_P, _F]),
     "kamino_step_host": (_I, [_P, _F, _P, _P, _P, _P, _P, _P, _SZ]),
+    "kamino_init_fbm": (_I, [_P]),
     "kamino_advection": (_I, [_P]),
     "kamino_geometric": (_I, [_P]),
     "kamino_projection": (_I, [_P]),

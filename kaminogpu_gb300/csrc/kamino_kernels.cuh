@@ -1727,6 +1727,78 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_vgrad(KGeo g, KBufs b, int uv_
     vgrad_tile2(g, b, uv_in, uv_out, q, q + ELEM_THREADS);
 }
 
+// ---------------------------------------------------------- FBM velocity
+// KaminoSolver::initialize_velocity and its FBM / interpNoise2D / rand
+// (KaminoInitializer.cu:3-134), on the device in the reference's arithmetic
+// (the reference runs it on the host): float for fReal, double where its
+// vec2 (double components), its lerp's 1.0 - alpha and the sin argument's
+// double literal make the expression double.  Rounded intrinsics keep every
+// float and double operation as written (no contraction).
+__device__ __forceinline__ float fbm_rand(double x, double y)
+{
+    const float dot = (float)__dadd_rn(__dmul_rn(x, 12.9898), __dmul_rn(y, 4.1414));
+    const float val = (float)sin(__dmul_rn((double)dot, 43758.5453));
+    return __fsub_rn(val, floorf(val));
+}
+__device__ __forceinline__ float fbm_lerp(float from, float to, float alpha)
+{
+    return (float)__dadd_rn(__dmul_rn(__dsub_rn(1.0, (double)alpha), (double)from), (double)__fmul_rn(alpha, to));
+}
+__device__ __forceinline__ float fbm_noise2(float x, float y)
+{
+    const float ix = floorf(x), fx = __fsub_rn(x, ix), iy = floorf(y), fy = __fsub_rn(y, iy);
+    const float ix1 = __fadd_rn(ix, 1.0f), iy1 = __fadd_rn(iy, 1.0f);
+    const float v1 = fbm_rand(ix, iy), v2 = fbm_rand(ix1, iy), v3 = fbm_rand(ix, iy1), v4 = fbm_rand(ix1, iy1);
+    return fbm_lerp(fbm_lerp(v1, v2, fx), fbm_lerp(v3, v4, fx), fy);
+}
+__device__ __forceinline__ float fbm(float x, float y)
+{
+    float total = 0.0f;
+    const float resX = (float)0.15, resY = (float)0.5;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const float freq = (float)(1 << i), amp = 1.0f / (float)(1 << i);  // pow(2, i), pow(0.5, i): exact
+        const float n = fbm_noise2(__fdiv_rn(__fmul_rn(x, freq), resX), __fdiv_rn(__fmul_rn(y, freq), resY));
+        total = __fadd_rn(total, __fmul_rn(amp, n));
+    }
+    return __fdiv_rn(__fmul_rn(0.5f, total), 2.0f);  // (1 - persistance) * total / 2
+}
+
+// u_phi[buf] (points 0 .. nt np - 1) and u_theta[buf] (the next (nt-1) np)
+__global__ void k_init_fbm(KGeo g, KBufs b, int buf)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nu = g.nt * g.np, nv = (g.nt - 1) * g.np;
+    if (t >= nu + nv) return;
+    const float h = g.h, h2 = __fdiv_rn(g.h, 2.0f), rg = __fmul_rn(g.R, g.h);
+    const float gain = (float)(4096.0 / (double)g.np);
+    if (t < nu) {
+        const int j = t / g.np, i = t - j * g.np;
+        float rx, lx;
+        if (i > 0) {
+            rx = __fadd_rn(__fmul_rn((float)i, h), h2);
+            lx = __fsub_rn(__fmul_rn((float)i, h), h2);
+        } else {  // the phi = 0 seam: the west points wrap to 2 pi
+            rx = h2;
+            lx = (float)__dsub_rn(2.0 * KAMINO_PI_D, (double)h2);
+        }
+        const float uy = __fmul_rn((float)(j + 1), h), ly = __fmul_rn((float)j, h);
+        const float nur = fbm(rx, uy), nlr = fbm(rx, ly), nul = fbm(lx, uy), nll = fbm(lx, ly);
+        const float dl = __fdiv_rn(__fsub_rn(nur, nlr), rg), dr = __fdiv_rn(__fsub_rn(nul, nll), rg);
+        const float avg = (float)__ddiv_rn((double)__fadd_rn(dl, dr), 2.0);
+        b.u[buf][t] = __fmul_rn(avg, gain);
+    } else {
+        const int k = t - nu, jr = k / g.np, i = k - jr * g.np, j = jr + 1;
+        // as the reference: the lower-left point sits at + h/2, like the upper-left
+        const float rx = __fmul_rn((float)(i + 1), h), lx = __fmul_rn((float)i, h);
+        const float jh = __fmul_rn((float)j, h), up = __fadd_rn(jh, h2), dn = __fsub_rn(jh, h2);
+        const float nur = fbm(rx, up), nlr = fbm(rx, dn), nul = fbm(lx, up), nll = fbm(lx, up);
+        const float du = __fdiv_rn(-__fsub_rn(nur, nul), rg), dd = __fdiv_rn(-__fsub_rn(nlr, nll), rg);
+        const float avg = (float)__ddiv_rn((double)__fadd_rn(du, dd), 2.0);
+        b.v[buf][k] = __fmul_rn(avg, gain);
+    }
+}
+
 // ------------------------------------------------------------- L2 flush
 // Eviction between timed steps: the buffer (larger than L2) is written, then
 // read, so the timed work starts from a cold L2 that holds no dirty lines;

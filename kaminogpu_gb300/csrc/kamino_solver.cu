@@ -907,6 +907,21 @@ extern "C" int kamino_step_host(kamino_handle h, float dt, const float* u_phi_in
     return KAMINO_OK;
 }
 
+// KaminoSolver::initialize_velocity (KaminoInitializer.cu:3-85; the
+// reference's constructor calls it, KaminoSolver.cu:59): u_phi and u_theta
+// from its FBM curl noise, computed on the device.
+extern "C" int kamino_init_fbm(kamino_handle h)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    const KGeo& g = h->g;
+    const int n = g.nt * g.np + (g.nt - 1) * g.np;
+    kk::k_init_fbm<<<(n + 255) / 256, 256, 0, h->stream>>>(g, h->b, h->cur_uv);
+    KCUDA(cudaGetLastError());
+    KCUDA(cudaStreamSynchronize(h->stream));
+    return KAMINO_OK;
+}
+
 extern "C" int kamino_set_state_device(kamino_handle h, int field, const float* dev, size_t pitch_bytes)
 {
     return copy_field(h, field, (void*)dev, pitch_bytes, true, cudaMemcpyDeviceToDevice, false);

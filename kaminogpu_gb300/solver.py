@@ -142,6 +142,10 @@ class KaminoSolver:
     def stepForward(self, dt=None):
         check(lib.kamino_step(self._h, self.config.dt if dt is None else dt))
 
+    def init_fbm(self):
+        """The reference's FBM curl-noise velocity (kamino_init_fbm)."""
+        check(lib.kamino_init_fbm(self._h))
+
     def step_host(self, u_phi, u_theta, thickness, dt=None):
         """One step with the state in host memory (kamino_step_host): uploads
         the three fields, steps, and returns the new three as arrays."""

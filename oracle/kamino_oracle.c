@@ -757,3 +757,82 @@ void oracle_ref_wrap(float *phi, float *theta, int64_t n, float h, int32_t *cell
         }
     }
 }
+
+/* ============================================================ FBM init
+ * KaminoSolver::initialize_velocity with its FBM / interpNoise2D / rand
+ * (KaminoInitializer.cu:3-134) in the reference's arithmetic: fReal is
+ * float; vec2 holds doubles (vectorUtil.cuh:9-24), so rand's dot product is
+ * double, rounded to float on assignment; the sin argument mixes a float
+ * and a double literal (double); kaminoLerpHost's (1.0 - alpha) makes its
+ * first product double; std::pow(float, int) returns double (exact powers of
+ * two here). */
+static float r_rand(double x, double y)
+{
+    const float dot = (float)(x * 12.9898 + y * 4.1414);
+    const float val = (float)sin((double)dot * 43758.5453);
+    return val - floorf(val);
+}
+static float r_lerp(float from, float to, float alpha)
+{
+    return (float)((1.0 - (double)alpha) * (double)from + (double)(alpha * to));
+}
+static float r_noise2(float x, float y)
+{
+    const float ix = floorf(x), fx = x - ix, iy = floorf(y), fy = y - iy;
+    const float v1 = r_rand(ix, iy), v2 = r_rand(ix + 1, iy), v3 = r_rand(ix, iy + 1), v4 = r_rand(ix + 1, iy + 1);
+    return r_lerp(r_lerp(v1, v2, fx), r_lerp(v3, v4, fx), fy);
+}
+static float r_fbm(float x, float y)
+{
+    float total = 0.0f;
+    const float resX = (float)0.15, resY = (float)0.5, pers = (float)0.5;
+    for (int i = 0; i < 4; i++) {
+        const float freq = (float)pow(2.0, i), amp = (float)pow((double)pers, i);
+        total += amp * r_noise2(x * freq / resX, y * freq / resY);
+    }
+    const float a = 1 - pers;
+    return a * total / 2.0f;
+}
+
+/* u_phi (nt rows) and u_theta (nt-1 rows) of nPhi = 2 nt columns; h is
+ * gridLen (float) and radius the float radius. */
+void oracle_ref_init_fbm(int nt, float radius, float h, float *u, float *v)
+{
+    const int np = 2 * nt;
+    const float gain = (float)(4096.0 / np);
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < nt; j++) {
+        for (int i = 0; i < np; i++) {
+            float urx, ury, lrx, lry, ulx, uly, llx, lly;
+            if (i > 0) {
+                urx = (float)i * h + h / 2;
+                ulx = (float)i * h - h / 2;
+            } else {  /* the phi = 0 seam: the west points wrap to 2 pi */
+                urx = h / 2;
+                ulx = (float)(2 * O_PI - (double)(h / 2));
+            }
+            lrx = urx;
+            llx = ulx;
+            ury = uly = (float)(j + 1) * h;
+            lry = lly = (float)j * h;
+            const float nur = r_fbm(urx, ury), nlr = r_fbm(lrx, lry), nul = r_fbm(ulx, uly), nll = r_fbm(llx, lly);
+            const float dl = (nur - nlr) / (radius * h), dr = (nul - nll) / (radius * h);
+            const float avg = (float)((double)(dl + dr) / 2.0);
+            u[(size_t)j * np + i] = avg * gain;
+        }
+    }
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j < nt; j++) {
+        for (int i = 0; i < np; i++) {
+            /* as the reference: the lower-left point sits at + h/2, like the upper-left */
+            const float urx = (float)(i + 1) * h, ury = (float)j * h + h / 2;
+            const float lrx = (float)(i + 1) * h, lry = (float)j * h - h / 2;
+            const float ulx = (float)i * h, uly = (float)j * h + h / 2;
+            const float llx = (float)i * h, lly = (float)j * h + h / 2;
+            const float nur = r_fbm(urx, ury), nlr = r_fbm(lrx, lry), nul = r_fbm(ulx, uly), nll = r_fbm(llx, lly);
+            const float du = -1 * (nur - nul) / (radius * h), dd = -1 * (nlr - nll) / (radius * h);
+            const float avg = (float)((double)(du + dd) / 2.0);
+            v[(size_t)(j - 1) * np + i] = avg * gain;
+        }
+    }
+}

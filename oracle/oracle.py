@@ -52,6 +52,7 @@ def _oracle_lib():
         L.oracle_set_threads.restype = _I
         L.oracle_ref_index.argtypes = [_I, _P, _P, _I64, _F, _I, _P, _P]
         L.oracle_ref_wrap.argtypes = [_P, _P, _I64, _F, _P]
+        L.oracle_ref_init_fbm.argtypes = [_I, _F, _F, _P, _P]
         _olib = L
     return _olib
 
@@ -157,6 +158,16 @@ def ref_index(kind, phi, theta, nt):
     L.oracle_ref_index(kind, phi.ctypes.data, theta.ctypes.data, n, grid_h(nt), nt, out.ctypes.data,
                        alpha.ctypes.data)
     return out, alpha
+
+
+def ref_init_fbm(nt, radius=1.0):
+    """u_phi, u_theta of KaminoSolver::initialize_velocity in the
+    reference's arithmetic (KaminoInitializer.cu:3-134)."""
+    L = _oracle_lib()
+    u = np.empty((nt, 2 * nt), np.float32)
+    v = np.empty((nt - 1, 2 * nt), np.float32)
+    L.oracle_ref_init_fbm(nt, radius, grid_h(nt), u.ctypes.data, v.ctypes.data)
+    return u, v
 
 
 def ref_wrap(phi, theta, nt):

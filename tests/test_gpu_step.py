@@ -192,3 +192,21 @@ def test_mid_size_with_particles(kg, orc):
     assert p.shape == (npart, 2)
     assert np.all((p[:, 0] >= 0) & (p[:, 0] <= np.float32(2 * np.pi))), "phi out of [0, 2pi]"
     assert np.all((p[:, 1] >= 0) & (p[:, 1] <= np.pi)), "theta out of [0, pi]"
+
+
+@pytest.mark.parametrize("nt", [64, 256])
+def test_fbm_velocity_init_vs_reference_arithmetic(kg, orc, nt):
+    """kamino_init_fbm (the reference's FBM curl-noise velocity, computed on
+    the device) against the oracle's restatement in the reference's host
+    arithmetic: equal bits except where the device and host double sin differ
+    in the last place and that shifts a float rounding."""
+    cfg = kg.default_config(n_theta=nt, radius=1.0, dt=0.005)
+    with kg.KaminoSolver(config=cfg) as s:
+        s.init_fbm()
+        gu, gv = s.get_state(kg.U_PHI), s.get_state(kg.U_THETA)
+    wu, wv = orc.ref_init_fbm(nt, 1.0)
+    for got, want in ((gu, wu), (gv, wv)):
+        assert np.all(np.isfinite(got))
+        same = np.mean(got.view(np.uint32) == want.view(np.uint32))
+        assert same >= 0.9999, same
+        assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max()

@@ -131,3 +131,68 @@ def test_fp64_oracle_vs_reference_kernels(orc, nt):
         d = np.abs(g[pre + "step%d_particles" % n].astype(np.float64) - f["particles"])
         d[:, 0] = np.minimum(d[:, 0], 2 * np.pi - d[:, 0])
         assert np.percentile(d, 99) < 1e-4, (n, np.percentile(d, 99))
+
+
+def _py_fbm_init(nt, radius=1.0):
+    """KaminoSolver::initialize_velocity written a second time, in Python:
+    np.float32 for the reference's float (fReal) operations, Python floats
+    for its double ones (KaminoInitializer.cu:3-134)."""
+    import math
+    f32 = np.float32
+
+    def rand(x, y):  # vec2 components are double
+        dot = f32(float(x) * 12.9898 + float(y) * 4.1414)
+        val = f32(math.sin(float(dot) * 43758.5453))
+        return f32(val - f32(math.floor(val)))
+
+    def lerp(a, b, t):
+        return f32((1.0 - float(t)) * float(a) + float(f32(t * b)))
+
+    def noise2(x, y):
+        ix, iy = f32(math.floor(x)), f32(math.floor(y))
+        fx, fy = f32(x - ix), f32(y - iy)
+        v1, v2 = rand(ix, iy), rand(f32(ix + f32(1)), iy)
+        v3, v4 = rand(ix, f32(iy + f32(1))), rand(f32(ix + f32(1)), f32(iy + f32(1)))
+        return lerp(lerp(v1, v2, fx), lerp(v3, v4, fx), fy)
+
+    def fbm(x, y):
+        total = f32(0)
+        for i in range(4):
+            freq, amp = f32(2.0 ** i), f32(0.5 ** i)
+            total = f32(total + f32(amp * noise2(f32(f32(x * freq) / f32(0.15)), f32(f32(y * freq) / f32(0.5)))))
+        return f32(f32(f32(0.5) * total) / f32(2))
+
+    h = f32(math.pi / nt)
+    np_, h2, rg, gain = 2 * nt, f32(h / f32(2)), f32(f32(radius) * h), f32(4096.0 / (2 * nt))
+    u = np.empty((nt, np_), np.float32)
+    v = np.empty((nt - 1, np_), np.float32)
+    for j in range(nt):
+        for i in range(np_):
+            if i > 0:
+                rx, lx = f32(f32(f32(i) * h) + h2), f32(f32(f32(i) * h) - h2)
+            else:
+                rx, lx = h2, f32(2 * math.pi - float(h2))
+            uy, ly = f32(f32(j + 1) * h), f32(f32(j) * h)
+            dl = f32(f32(fbm(rx, uy) - fbm(rx, ly)) / rg)
+            dr = f32(f32(fbm(lx, uy) - fbm(lx, ly)) / rg)
+            u[j, i] = f32(f32(float(f32(dl + dr)) / 2.0) * gain)
+    for j in range(1, nt):
+        for i in range(np_):
+            rx, lx = f32(f32(i + 1) * h), f32(f32(i) * h)
+            jh = f32(f32(j) * h)
+            up, dn = f32(jh + h2), f32(jh - h2)
+            du = f32(-f32(fbm(rx, up) - fbm(lx, up)) / rg)
+            dd = f32(-f32(fbm(rx, dn) - fbm(lx, up)) / rg)
+            v[j - 1, i] = f32(f32(float(f32(du + dd)) / 2.0) * gain)
+    return u, v
+
+
+def test_fbm_init_restatements_agree(orc):
+    """The oracle's C restatement of the reference's FBM velocity initialiser
+    against a second one in Python (nTheta = 16), bit for bit."""
+    u, v = orc.ref_init_fbm(16, 1.0)
+    pu, pv = _py_fbm_init(16, 1.0)
+    assert np.all(np.isfinite(u)) and np.all(np.isfinite(v))
+    assert np.array_equal(u.view(np.uint32), pu.view(np.uint32))
+    assert np.array_equal(v.view(np.uint32), pv.view(np.uint32))
+    assert np.abs(u).max() > 0 and np.abs(v).max() > 0
