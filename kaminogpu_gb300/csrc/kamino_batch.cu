@@ -100,10 +100,10 @@ __global__ void __launch_bounds__(kk::ELEM_THREADS) kb_geo(const KSphere* __rest
     }
 }
 
-// The FFT and solve stages come in three instances by the batch's largest
-// nTheta (MAXN = 256, 1024, 2048): a batch of small spheres does not run
-// code sized, in registers, for the 2048-row tiles (the 256 class is held
-// to 128 registers).
+// The FFT and solve stages come in two instances by the batch's largest
+// nTheta (MAXN = 256, 1024; batched spheres have nTheta <= 1024): a batch of
+// small spheres does not run code sized, in registers, for the 1024-row
+// tiles (the 256 class is held to 128 registers).
 constexpr int fft_stage_min_ctas(int maxn) { return maxn <= 256 ? 2 : 1; }
 template <int MAXN>
 __global__ void __launch_bounds__(kk::FFT_MAX_THREADS, fft_stage_min_ctas(MAXN)) kb_div_fft(const KSphere* __restrict__ sph,
@@ -146,20 +146,11 @@ __global__ void __launch_bounds__(kk::FFT_MAX_THREADS, fft_stage_min_ctas(MAXN))
 using FftStageKernel = void (*)(const KSphere*, const int2*, int, int*, int, int);
 using SolveStageKernel = void (*)(const KSphere*, const int2*, int, int*);
 
-// smallest size class (256, 1024, 2048) holding nTheta = nt
-inline int size_class(int nt) { return nt <= 256 ? 256 : (nt <= 1024 ? 1024 : 2048); }
-inline FftStageKernel div_stage(int cls)
-{
-    return cls == 256 ? kb_div_fft<256> : (cls == 1024 ? kb_div_fft<1024> : kb_div_fft<2048>);
-}
-inline FftStageKernel ifft_stage(int cls)
-{
-    return cls == 256 ? kb_ifft<256> : (cls == 1024 ? kb_ifft<1024> : kb_ifft<2048>);
-}
-inline SolveStageKernel solve_stage(int cls)
-{
-    return cls == 256 ? kb_solve<256> : (cls == 1024 ? kb_solve<1024> : kb_solve<2048>);
-}
+// smallest size class (256, 1024) holding nTheta = nt
+inline int size_class(int nt) { return nt <= 256 ? 256 : 1024; }
+inline FftStageKernel div_stage(int cls) { return cls == 256 ? kb_div_fft<256> : kb_div_fft<1024>; }
+inline FftStageKernel ifft_stage(int cls) { return cls == 256 ? kb_ifft<256> : kb_ifft<1024>; }
+inline SolveStageKernel solve_stage(int cls) { return cls == 256 ? kb_solve<256> : kb_solve<1024>; }
 
 __global__ void __launch_bounds__(kk::ELEM_THREADS) kb_vgrad(const KSphere* __restrict__ sph,
                                                               const int2* __restrict__ items, int n, int* counter,
@@ -201,7 +192,7 @@ struct Engine {
     size_t smem_fft = 0, smem_solve = 0;
     int fft_block = 128;  // threads of the FFT kernels: the largest sphere's fft_threads
     int fft_resident = 1; // FFT CTAs of that size resident per SM (registers, shared memory)
-    int cls = 2048;       // size class of the FFT and solve kernels: the largest sphere's
+    int cls = 1024;       // size class of the FFT and solve kernels: the largest sphere's
     Shapes shapes;
     int cu = 0, cr = 0;
     cudaGraphExec_t graph[2][2] = {};
@@ -328,7 +319,7 @@ struct Engine {
             max_nt = std::max(max_nt, nt);
         }
         cls = size_class(max_nt);
-        for (int c : {256, 1024, 2048}) {  // attributes belong to the functions, shared by every engine
+        for (int c : {256, 1024}) {  // attributes belong to the functions, shared by every engine
             BCUDA(cudaFuncSetAttribute(div_stage(c), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)kk::fft_smem_max()));
             BCUDA(cudaFuncSetAttribute(ifft_stage(c), cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -889,7 +880,7 @@ extern "C" int kamino_server_poll(kamino_server s, int* n_completed)
         auto r = *qi;
         if (r->arrival > t) break;
         if (s->cfg.max_resident > 0 && (int)s->resident.size() >= s->cfg.max_resident) break;
-        const bool solo = r->cfg.n_theta >= s->solo_n_theta();
+        const bool solo = r->cfg.n_theta >= s->solo_n_theta() || r->cfg.n_theta > 1024;  // batched: <= 1024
         if (solo && solo_free <= 0) {
             ++qi;
             continue;

@@ -155,3 +155,4 @@ def test_batch_matches_solo_bitwise_large(kg, fp64):
             bad = [k for k, f in (("u_phi", kg.U_PHI), ("u_theta", kg.U_THETA), ("thickness", kg.THICKNESS))
                    if not np.array_equal(b.get_state(i, f).view(np.uint32), want[k].view(np.uint32))]
             assert not bad, (nt, bad)
+

@@ -41,7 +41,7 @@ def test_stage_vs_fp64_oracle(kg, orc, nt, stage):
 
 @pytest.mark.parametrize("nt,dt,steps,lmax", [(32, 0.005, 1, 8), (32, 0.005, 100, 8), (128, 0.005, 1, 8),
                                               (128, 0.005, 100, 8), (256, 0.002, 100, 16),
-                                              (1024, 0.001, 1, 32)])
+                                              (1024, 0.001, 1, 32), (2048, 0.0005, 1, 32)])
 def test_step_vs_fp64_oracle(kg, orc, nt, dt, steps, lmax):
     st, s, o = make_pair(kg, orc, nt, dt, lmax=lmax, vortex=nt >= 1024)
     s.step_n(steps)
