@@ -38,8 +38,14 @@ constexpr int SOLVE_THREADS = 128;  // threads of a k_solve CTA (one tile of Fou
 // scheduled while the previous kernel on the stream drains; each begins with
 // pdl_wait() (PTX griddepcontrol.wait), which returns once the previous grid
 // has completed and its writes are visible, and is a no-op for a normal
-// launch.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// launch.  It then lets the next kernel be scheduled
+// (griddepcontrol.launch_dependents): that one launches once every CTA of
+// this grid has started, and waits in its own pdl_wait for this grid to end.
+__device__ __forceinline__ void pdl_wait()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
 
 template <typename... KArgs, typename... Args>
 inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
