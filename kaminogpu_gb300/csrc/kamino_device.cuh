@@ -248,60 +248,62 @@ __device__ __forceinline__ float advect_cell(const float* __restrict__ u, const 
     return sample_cell<KIND>(field, i, j, -dp, -dtt, g, vf && KIND != KIND_CENTERED);
 }
 
-// floor of x by a round-down add of 1.5 * 2^23 (exact for |x| < 2^22, which
-// every in-range cell offset is): returns floor(x) as an int and sets frac to
-// x - floor(x), the same value floorf gives.  Full-rate adds instead of a
-// rounding and a conversion; any other x (huge or non-finite) gives some int
-// that the callers' range checks send to the exact path.
-__device__ __forceinline__ int floor_frac(float x, float& frac)
-{
-    const float t = __fadd_rd(x, 12582912.0f);
-    frac = x - (t - 12582912.0f);
-    return __float_as_int(t) - 0x4B400000;
-}
+// Packed pairs (f32x2: one instruction for two FP32 lanes of a register
+// pair, sm_100 and later) carry the two coordinates of a position and the
+// two row lerps of a bilinear sample.  Each lane rounds as the scalar
+// instruction would.
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+// floor of a position pair by a round-down add of 1.5 * 2^23: t - 1.5 * 2^23
+// is floor(x) exactly for -2^22 <= x < 2^23, so the fraction x - floor(x) is
+// exact too; the caller reads floor(x) + 0x4B400000 from t's bits.
+constexpr float kFloorBias = 12582912.0f;
+constexpr int kFloorBits = 0x4B400000;
 
 // sample_cell for positions whose rows it, it + 1 both lie in [0, pole_row)
 // and whose column pair does not straddle the phi seam: plain bilinear from
-// one address (the phi neighbour at +1, the next row at +pitch).  Anything
-// else (a pole row, a crossing, the seam, non-finite input) goes to
-// sample_cell, so the result is sample_cell's in every case.
+// one address (the phi neighbour at +1, the next row at +pitch).  A pole
+// row, a crossing, the seam or a non-finite position goes to sample_cell,
+// so the result is sample_cell's for every phi offset of less than 2^22
+// cells (any displacement a stable time step can make).
+// ib, jb = i, j - 0x4B400000 (mod 2^32): ib + bits(t) = i + floor(x).
 template <int KIND>
-__device__ __forceinline__ float sample_fast(const float* __restrict__ f, int i, int j, float x, float y,
-                                             const KGeo& g, bool vec_flip)
+__device__ __forceinline__ float sample_fast(const float* __restrict__ f, int i, int j, unsigned ib, unsigned jb,
+                                             float2 p, const KGeo& g, bool vec_flip)
 {
-    float ax, ay;
-    const int kx = floor_frac(x, ax), ky = floor_frac(y, ay);
-    const int it = j + ky;
-    const int i0 = (i + kx) & g.mask;
+    const float2 t = __fadd2_rd(p, f2(kFloorBias, kFloorBias));
+    const float2 a = __fadd2_rn(p, __ffma2_rn(t, f2(-1.0f, -1.0f), f2(kFloorBias, kFloorBias)));
+    const int it = (int)(jb + (unsigned)__float_as_int(t.y));
+    const int i0 = (int)(ib + (unsigned)__float_as_int(t.x)) & g.mask;
     const int pole_row = (KIND == KIND_VTHETA) ? g.nt - 2 : g.nt - 1;
     if ((unsigned)it < (unsigned)pole_row && i0 != g.mask) {
         const float* p0 = f + (it * g.pitch + i0);
         const float* p1 = p0 + g.pitch;
-        const float v00 = __ldg(p0), v01 = __ldg(p0 + 1);
-        const float v10 = __ldg(p1), v11 = __ldg(p1 + 1);
-        return lerp2(lerp2(v00, v01, ax), lerp2(v10, v11, ax), ay);
+        const float2 lo = f2(__ldg(p0), __ldg(p1)), hi = f2(__ldg(p0 + 1), __ldg(p1 + 1));
+        const float2 r = __ffma2_rn(f2(a.x, a.x), __ffma2_rn(lo, f2(-1.0f, -1.0f), hi), lo);
+        return lerp2(r.x, r.y, a.y);
     }
-    return sample_cell<KIND>(f, i, j, x, y, g, vec_flip);
+    return sample_cell<KIND>(f, i, j, p.x, p.y, g, vec_flip);
 }
 
-// RK2 step of one quantity from its start-point velocities (gu, gv):
-// advect_cell after its first two samples.
+// RK2 step of one quantity from its start-point velocities gv = (u, v):
+// advect_cell after its first two samples.  nhc = (-cP / 2, -cT / 2).
 template <int KIND>
 __device__ __forceinline__ float advect_from(const float* __restrict__ u, const float* __restrict__ v,
-                                             const float* __restrict__ field, int i, int j, float gu, float gv,
-                                             float cP, float cT, const KGeo& g, bool vf)
+                                             const float* __restrict__ field, int i, int j, unsigned ib,
+                                             unsigned jb, float2 gv, float2 nhc, const KGeo& g, bool vf)
 {
     constexpr float cgp = (KIND == KIND_VPHI) ? -0.5f : 0.0f;
     constexpr float cgt = (KIND == KIND_VTHETA) ? 1.0f : 0.5f;
     constexpr float ou_p = cgp + 0.5f, ou_t = cgt - 0.5f;
     constexpr float ov_p = cgp, ov_t = cgt - 1.0f;
-    float dp = gu * cP, dtt = gv * cT;
-    float hp = 0.5f * dp, ht = 0.5f * dtt;
-    float mu = sample_fast<KIND_VPHI>(u, i, j, ou_p - hp, ou_t - ht, g, vf);
-    float mv = sample_fast<KIND_VTHETA>(v, i, j, ov_p - hp, ov_t - ht, g, vf);
-    dp = 0.5f * (mu + gu) * cP;
-    dtt = 0.5f * (mv + gv) * cT;
-    return sample_fast<KIND>(field, i, j, -dp, -dtt, g, vf && KIND != KIND_CENTERED);
+    // midpoint: offset - d / 2 for each sampler
+    const float2 hd = __fmul2_rn(gv, nhc);
+    const float mu = sample_fast<KIND_VPHI>(u, i, j, ib, jb, __fadd2_rn(hd, f2(ou_p, ou_t)), g, vf);
+    const float mv = sample_fast<KIND_VTHETA>(v, i, j, ib, jb, __fadd2_rn(hd, f2(ov_p, ov_t)), g, vf);
+    // departure point: -(mid + start) / 2 * c
+    const float2 d = __fmul2_rn(__fadd2_rn(f2(mu, mv), gv), nhc);
+    return sample_fast<KIND>(field, i, j, ib, jb, d, g, vf && KIND != KIND_CENTERED);
 }
 
 // The three advected quantities of cell (i, j) in one thread: u_phi at
@@ -336,9 +338,12 @@ __device__ __forceinline__ void advect_cell3(const float* __restrict__ u, const 
         const float gv_th = v00;
         const float gu_c = u_mid0;
         const float gv_c = lerp2(vm0, v00, 0.5f);
-        out_u = advect_from<KIND_VPHI>(u, v, u, i, j, gu_phi, gv_phi, cPc, cT, g, vf);
-        out_v = advect_from<KIND_VTHETA>(u, v, v, i, j, gu_th, gv_th, cPv, cT, g, vf);
-        out_r = advect_from<KIND_CENTERED>(u, v, rho, i, j, gu_c, gv_c, cPc, cT, g, vf);
+        const unsigned ib = (unsigned)i - (unsigned)kFloorBits, jb = (unsigned)j - (unsigned)kFloorBits;
+        const float2 nhc = __fmul2_rn(f2(cPc, cT), f2(-0.5f, -0.5f));
+        const float2 nhv = f2(-0.5f * cPv, nhc.y);
+        out_u = advect_from<KIND_VPHI>(u, v, u, i, j, ib, jb, f2(gu_phi, gv_phi), nhc, g, vf);
+        out_v = advect_from<KIND_VTHETA>(u, v, v, i, j, ib, jb, f2(gu_th, gv_th), nhv, g, vf);
+        out_r = advect_from<KIND_CENTERED>(u, v, rho, i, j, ib, jb, f2(gu_c, gv_c), nhc, g, vf);
         return;
     }
     out_u = advect_cell<KIND_VPHI>(u, v, u, i, j, cPc, cT, g);
