@@ -383,7 +383,7 @@ __device__ __forceinline__ double ref_solve_cubic64(double b, double c)
     return A + B;
 }
 
-// The FP64 branch of geo_root (1 + G v <= 0).  Not inlined, so none of its
+// The FP64 branch of geo_roots (1 + G v <= 0).  Not inlined, so none of its
 // double arithmetic is evaluated ahead of the branch for every cell (FP64 is
 // 1/64 of the FP32 rate on GB300).
 static __device__ __noinline__ float geo_root_fp64(float G, float uPrev, float vPrev)
@@ -392,31 +392,52 @@ static __device__ __noinline__ float geo_root_fp64(float G, float uPrev, float v
     return (float)ref_solve_cubic64(((double)G * vPrev + 1.0) / G2, -(double)uPrev / G2);
 }
 
-// u' of geometricFillKernel (KaminoCore.cu:494-508): the root the reference
-// takes of u^3 + ((G v + 1)/G^2) u - uPrev/G^2 = 0.  When 1 + G v > 0 that
-// root is unique and g(u) = G^2 u^3 + (1 + G v) u - uPrev is increasing and
+// u' of geometricFillKernel (KaminoCore.cu:494-508) for N cells of one row
+// (one G): the root the reference takes of
+// u^3 + ((G v + 1)/G^2) u - uPrev/G^2 = 0.  When 1 + G v > 0 that root is
+// unique and g(u) = G^2 u^3 + (1 + G v) u - uPrev is increasing and
 // convex/concave on either side of 0, so Newton from uPrev/(1 + G v)
 // converges monotonically; FP32 keeps full relative accuracy (the
 // reference's FP32 Cardano form cancels A + B catastrophically near the
-// equator, where G is small).
-__device__ __forceinline__ float geo_root(float G, float uPrev, float vPrev)
+// equator, where G is small).  The N Newton iterations run in lockstep (N
+// independent dependency chains in flight), each cell's x frozen from the
+// iteration its own test stops it, so a root does not depend on N.  For
+// every cell that iterates, df >= 1 + G v > 0.
+template <int N>
+__device__ __forceinline__ void geo_roots(float G, const float (&uPrev)[N], const float (&vPrev)[N], float (&x)[N])
 {
-    if (!(fabsf(G) > 1e-7f)) return uPrev;
-    float a = __fmaf_rn(G, vPrev, 1.0f);
-    if (a > 0.0f) {
-        float G2 = G * G;
-        float x = uPrev * rcp_approx(a);
-        for (int k = 0; k < 40; k++) {
-            float x2 = x * x;
-            float f = __fmaf_rn(G2 * x2, x, __fmaf_rn(a, x, -uPrev));
-            float df = __fmaf_rn(3.0f * G2, x2, a);
-            float dx = f * rcp_approx(df);  // df >= a > 0
-            x -= dx;
-            if (!(fabsf(dx) > 5e-7f * fabsf(x))) break;
-        }
-        return x;
+    if (!(fabsf(G) > 1e-7f)) {
+#pragma unroll
+        for (int k = 0; k < N; k++) x[k] = uPrev[k];
+        return;
     }
-    return geo_root_fp64(G, uPrev, vPrev);
+    const float G2 = G * G;
+    float a[N];
+    bool live[N];
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+        a[k] = __fmaf_rn(G, vPrev[k], 1.0f);
+        live[k] = a[k] > 0.0f;
+        x[k] = live[k] ? uPrev[k] * rcp_approx(a[k]) : 0.0f;
+    }
+    for (int it = 0; it < 40; it++) {
+        bool any = false;
+#pragma unroll
+        for (int k = 0; k < N; k++) {
+            const float x2 = x[k] * x[k];
+            const float f = __fmaf_rn(G2 * x2, x[k], __fmaf_rn(a[k], x[k], -uPrev[k]));
+            const float df = __fmaf_rn(3.0f * G2, x2, a[k]);
+            const float dx = f * rcp_approx(df);
+            const float xn = x[k] - dx;
+            if (live[k]) x[k] = xn;
+            live[k] = live[k] && fabsf(dx) > 5e-7f * fabsf(xn);
+            any |= live[k];
+        }
+        if (!any) break;
+    }
+#pragma unroll
+    for (int k = 0; k < N; k++)
+        if (!(a[k] > 0.0f)) x[k] = geo_root_fp64(G, uPrev[k], vPrev[k]);
 }
 
 // ------------------------------------------------------- complex product

@@ -232,14 +232,12 @@ __device__ __forceinline__ void geo_tile(const KGeo& g, const KBufs& b, int src,
     }
     const float uu[ELEM_VEC + 1] = {uc.x, uc.y, uc.z, uc.w, un};
     const float G = __ldg(b.gfac + j);
-    float cu[ELEM_VEC], cv[ELEM_VEC];
+    float up[ELEM_VEC], cu[ELEM_VEC], cv[ELEM_VEC];
 #pragma unroll
-    for (int k = 0; k < ELEM_VEC; k++) {
-        const float uPrev = 0.5f * __fadd_rn(uu[k], uu[k + 1]);
-        const float uNext = geo_root(G, uPrev, vp[k]);
-        cu[k] = uNext;
-        cv[k] = __fadd_rn(vp[k], __fmul_rn(__fmul_rn(G, uNext), uNext));
-    }
+    for (int k = 0; k < ELEM_VEC; k++) up[k] = 0.5f * __fadd_rn(uu[k], uu[k + 1]);
+    geo_roots<ELEM_VEC>(G, up, vp, cu);
+#pragma unroll
+    for (int k = 0; k < ELEM_VEC; k++) cv[k] = __fadd_rn(vp[k], __fmul_rn(__fmul_rn(G, cu[k]), cu[k]));
     *reinterpret_cast<float4*>(b.cu + idx) = make_float4(cu[0], cu[1], cu[2], cu[3]);
     *reinterpret_cast<float4*>(b.cv + idx) = make_float4(cv[0], cv[1], cv[2], cv[3]);
 }
