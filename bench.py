@@ -260,9 +260,77 @@ def run_ours(args, ws, rank, local, dist):
         out["batched"] = bench_batched(kg, local)
     if not args.no_served:
         out["served"] = bench_served(kg, local, args.served_seconds)
+    if not args.no_frames:
+        out["frame_output"] = bench_frames(kg, local, st, hbm)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(st, seconds=10.0)
     return out
+
+
+def bench_frames(kg, local, st, hbm, frames=5, steps_per_frame=10):
+    """.bgeo frame output of the nTheta=1024 sphere (write_data_bgeo,
+    KaminoSolver.cu:284-357): the device pack kernel against the HBM roofline
+    (12 B read + 32 B written per cell), and the frame loop with output
+    (kamino_run_frames_bgeo: pack, copy and file write overlapping the next
+    frame's steps) against the same frames with no output and against the
+    reference's order (wait, copy the fields back, pack on the host with one
+    thread, write; the oracle's restatement does the packing)."""
+    import shutil
+    import tempfile
+
+    from oracle import oracle as orc
+    dt_frame = DT * steps_per_frame  # the frame loop takes about steps_per_frame + 1 steps a frame
+    cfg = kg.default_config(n_theta=NT, radius=1.0, dt=DT, fp64_modes=4, device=local)
+    cfg.frame_dt = dt_frame
+    s = kg.KaminoSolver(config=cfg)
+    s.load(st)
+    C = NT * 2 * NT
+    pack_ms = s.time_frame_pack(kg.FRAME_GRID, reps=20, flush_l2=True)
+    pack_bytes = 44 * C
+    tmp = tempfile.mkdtemp(prefix="kamino_frames_")
+    try:
+        s.run_frames_bgeo(1, os.path.join(tmp, "warm_"))  # first-use buffers
+        s.load(st)
+        s.synchronize()
+        t0 = time.perf_counter()
+        steps = s.run_frames_bgeo(frames, os.path.join(tmp, "grid_"))
+        wall_out = time.perf_counter() - t0
+        s.load(st)
+        s.synchronize()
+        t0 = time.perf_counter()
+        s.run_frames(frames)
+        s.synchronize()
+        wall_none = time.perf_counter() - t0
+        s.load(st)
+        threads = orc.set_threads(1)
+        per_frame = [kg.frame_steps(DT, dt_frame, i) - kg.frame_steps(DT, dt_frame, i - 1)
+                     for i in range(1, frames + 1)]
+        t0 = time.perf_counter()
+        for i in range(frames + 1):
+            if i:
+                s.step_n(per_frame[i - 1])
+            f = s.fields()
+            img = orc.bgeo_image(orc.frame_grid_records(f["u_phi"], f["u_theta"], f["thickness"], NT, 1.0),
+                                 orc.GRID_ATTRS)
+            with open(os.path.join(tmp, "host_%d.bgeo" % i), "wb") as fp:
+                fp.write(img)
+        wall_host = time.perf_counter() - t0
+        orc.set_threads(os.cpu_count() or 1)
+        same = open(os.path.join(tmp, "grid_%d.bgeo" % frames), "rb").read(41) == img[:41]
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    nbytes = s.frame_bytes(kg.FRAME_GRID)
+    s.close()
+    achieved = pack_bytes / (pack_ms / 1e3) / 1e9
+    return {"workload": "nTheta=1024 sphere, %d frames of frame_dt = %d dt (%d steps in all), grid .bgeo per "
+                        "frame (%.1f MB)" % (frames, steps_per_frame, steps, nbytes / 1e6),
+            "steps": steps, "pack_kernel": {"avg_launch_ms": pack_ms, "algorithmic_bytes_per_launch": pack_bytes,
+                                            "achieved": achieved, "peak": hbm, "frac": achieved / hbm,
+                                            "unit": "GB/s"},
+            "frames_with_output_s_per_frame": wall_out / frames,
+            "frames_without_output_s_per_frame": wall_none / frames,
+            "host_packing_order_s_per_frame": wall_host / frames, "host_packing_threads": threads,
+            "headers_equal": same}
 
 
 def _same(a, b):
@@ -545,6 +613,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-frames", action="store_true")
     ap.add_argument("--served-seconds", type=float, default=5.0)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -207,6 +207,49 @@ int kamino_step_n(kamino_handle h, int n);
  * every step uses the configured dt as the reference does (N5). */
 int kamino_run_frames(kamino_handle h, int frames, int64_t* steps_taken);
 
+/* ------------------------------------------------------------ frame output
+ * The .bgeo files Kamino writes after every frame, through Partio's
+ * uncompressed BGEO writer (Houdini classic geometry, big-endian):
+ *   KAMINO_FRAME_GRID       KaminoSolver::write_data_bgeo
+ *                           (KaminoSolver.cu:284-357): one point per cell
+ *                           centre, attributes position, v (the centred
+ *                           velocity mapped to 3-D, mapVToSphere :409-423)
+ *                           and density (the thickness);
+ *   KAMINO_FRAME_PARTICLES  KaminoSolver::write_particles_bgeo (:359-396):
+ *                           one point per particle, position, v = 0 and
+ *                           color (0: the reference's colours come from its
+ *                           image input, which is not built).
+ * The records are computed on the device in the file's byte order and
+ * copied to pinned host memory on a second stream, so work issued after a
+ * capture overlaps the copy. */
+enum kamino_frame_kind { KAMINO_FRAME_GRID = 0, KAMINO_FRAME_PARTICLES = 1 };
+
+/* Size of the file a frame of this kind writes. */
+int kamino_frame_bytes(kamino_handle h, int kind, size_t* bytes);
+
+/* Snapshot the current state as a frame: queues the pack kernel on the
+ * handle's stream and the device->host copy behind it; returns at once.  At
+ * most two captures of a kind wait to be written (a third is an error). */
+int kamino_frame_capture(kamino_handle h, int kind);
+
+/* Waits for the oldest captured frame of the kind (capturing the current
+ * state first if none waits) and writes its file image to path (if not
+ * NULL) and to host (if not NULL; host_bytes >= kamino_frame_bytes). */
+int kamino_frame_write(kamino_handle h, int kind, const char* path, void* host, size_t host_bytes);
+
+/* Kamino::run (KaminoCore.cu:860-912) with its output: writes frame 0, then
+ * runs every frame's steps (as kamino_run_frames) and writes
+ * <grid_path><i>.bgeo and <particle_path><i>.bgeo (a NULL or empty path
+ * skips that kind).  Frame i's file is written while the GPU runs frame
+ * i+1. */
+int kamino_run_frames_bgeo(kamino_handle h, int frames, const char* grid_path, const char* particle_path,
+                           int64_t* steps_taken);
+
+/* Device time of one pack kernel launch of the kind, averaged over reps
+ * (CUDA events on the handle's stream; flush_l2 evicts the L2 before each
+ * launch, outside the timed interval). */
+int kamino_frame_time_pack(kamino_handle h, int kind, int reps, int flush_l2, double* ms);
+
 int kamino_synchronize(kamino_handle h);
 
 /* Elapsed simulated time (KaminoSolver.cu:220) and step count. */

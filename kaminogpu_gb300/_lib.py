@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(_HERE, "lib", "libkamino_gb300.so")
 OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_IO, ERR_BUDGET, ERR_TIMEOUT, ERR_NOT_READY, ERR_NOT_FOUND = range(9)
 # fields (enum kamino_field)
 U_PHI, U_THETA, THICKNESS, PRESSURE, PARTICLES = range(5)
+FRAME_GRID, FRAME_PARTICLES = range(2)
 # flags (enum kamino_flags)
 F_PARTICLE_RK2, F_POLE_SIGN_FLIP, F_HONOR_STEP_DT, F_NO_PRESSURE_OUT, F_REFERENCE_ROUNDING = 1, 2, 4, 8, 16
 
@@ -124,6 +125,11 @@ SIGNATURES = {
     "kamino_step_n": (_I, [_P, _I]),
     "kamino_projection_noalloc": (_I, [_I, _P, _P, _P, _P, _P, _P]),
     "kamino_run_frames": (_I, [_P, _I, ctypes.POINTER(_I64)]),
+    "kamino_frame_bytes": (_I, [_P, _I, ctypes.POINTER(_SZ)]),
+    "kamino_frame_capture": (_I, [_P, _I]),
+    "kamino_frame_write": (_I, [_P, _I, ctypes.c_char_p, _P, _SZ]),
+    "kamino_run_frames_bgeo": (_I, [_P, _I, ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_I64)]),
+    "kamino_frame_time_pack": (_I, [_P, _I, _I, _I, ctypes.POINTER(_D)]),
     "kamino_synchronize": (_I, [_P]),
     "kamino_time_elapsed": (_I, [_P, ctypes.POINTER(_D), ctypes.POINTER(_I64)]),
     "kamino_time_steps": (_I, [_P, _I, _I, ctypes.POINTER(_D)]),

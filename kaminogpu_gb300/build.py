@@ -16,7 +16,7 @@ LIB = os.path.join(OUT, "libkamino_gb300.so")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-UNITS = ["kamino_solver.cu", "kamino_batch.cu", "kamino_noalloc.cu", "kamino_init.cpp"]
+UNITS = ["kamino_solver.cu", "kamino_batch.cu", "kamino_noalloc.cu", "kamino_frames.cu", "kamino_init.cpp"]
 
 
 def _newest_header():

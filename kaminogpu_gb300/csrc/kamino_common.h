@@ -39,6 +39,16 @@ int kamino_internal_set_counters(kamino_handle h, int cur_uv, int cur_r, int64_t
 int kamino_internal_reset(kamino_handle h, const kamino_config* cfg);
 // The handle's own stream (its steps and copies are ordered on it).
 cudaStream_t kamino_internal_stream(kamino_handle h);
+// The handle's configuration as created.
+int kamino_internal_config(kamino_handle h, kamino_config* cfg);
+// Evicts the L2 on the handle's stream (a write and a read of a buffer larger
+// than L2), for timing entry points.
+int kamino_internal_flush_l2(kamino_handle h);
+// Frame output (kamino_frames.cu): the handle's frame state, made current
+// with the handle's device; released by kamino_destroy.
+struct KFrames;
+int kamino_internal_frames(kamino_handle h, KFrames*** out);
+void kamino_frames_release(KFrames* f);
 
 #define KAMINO_PI_D 3.14159265358979323846   /* M_PI  (KaminoHeader.cuh:26) */
 #define KAMINO_2PI_D 6.28318530717958647692  /* M_2PI (KaminoHeader.cuh:27) */

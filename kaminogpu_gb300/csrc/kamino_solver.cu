@@ -60,6 +60,7 @@ struct kamino_solver_s {
     size_t smem_div = 0, smem_solve = 0, smem_ifft = 0;
     cudaStream_t io_stream = nullptr;  // kamino_step_host: the early thickness download
     cudaEvent_t ev_adv = nullptr;      // kamino_step_host: the advection has written its fields
+    KFrames* frames = nullptr;         // frame output (kamino_frames.cu), made on first use
 };
 
 static const char* const kKernelNames[] = {"k_advect", "k_geo_centers", "k_div_fft",
@@ -144,6 +145,7 @@ extern "C" int kamino_destroy(kamino_handle h)
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     destroy_graphs(h);
+    kamino_frames_release(h->frames);
     if (h->io_stream) cudaStreamSynchronize(h->io_stream);
     if (h->ev_adv) cudaEventDestroy(h->ev_adv);
     if (h->io_stream) cudaStreamDestroy(h->io_stream);
@@ -716,6 +718,21 @@ int kamino_internal_set_counters(kamino_handle h, int cur_uv, int cur_r, int64_t
 
 cudaStream_t kamino_internal_stream(kamino_handle h) { return h ? h->stream : nullptr; }
 
+int kamino_internal_frames(kamino_handle h, KFrames*** out)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    *out = &h->frames;
+    return KAMINO_OK;
+}
+
+int kamino_internal_config(kamino_handle h, kamino_config* cfg)
+{
+    if (!h) return kamino_fail(KAMINO_ERR_INVALID, "null handle");
+    *cfg = h->cfg;
+    return KAMINO_OK;
+}
+
 int kamino_internal_reset(kamino_handle h, const kamino_config* cfg)
 {
     int rc = check_handle(h);
@@ -943,6 +960,15 @@ static int ensure_flush(kamino_solver_s* h)
         h->flush = nullptr;
         return kamino_fail(KAMINO_ERR_ALLOC, "L2 flush buffer: %s", cudaGetErrorString(e));
     }
+    return KAMINO_OK;
+}
+
+int kamino_internal_flush_l2(kamino_handle h)
+{
+    int rc = check_handle(h);
+    if (!rc) rc = ensure_flush(h);
+    if (rc) return rc;
+    KCUDA(kk::flush_l2(h->flush, h->flush_bytes, 0, h->stream));
     return KAMINO_OK;
 }
 

@@ -6,6 +6,7 @@ KaminoSolver keeps the reference's constructor and method names
   stepForward(dt)                           KaminoSolver.cu:197-221
   advection() / geometric() / projection()  KaminoCore.cu:344, 551, 749
   copyToGPU / copyBackToCPU per field       KaminoQuantity.cu:3-18
+  write_data_bgeo / write_particles_bgeo    KaminoSolver.cu:284-396
 Errors raise KaminoError instead of exiting the process.
 """
 import ctypes
@@ -13,7 +14,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import (PARTICLES, PRESSURE, THICKNESS, U_PHI, U_THETA, KaminoConfig, KaminoInitSpec, check,
+from ._lib import (FRAME_GRID, FRAME_PARTICLES, PARTICLES, PRESSURE, THICKNESS, U_PHI, U_THETA, KaminoConfig, KaminoInitSpec, check,
                    lib)
 
 _FIELD_NAMES = {"velPhi": U_PHI, "velTheta": U_THETA, "density": THICKNESS, "thickness": THICKNESS,
@@ -177,6 +178,45 @@ class KaminoSolver:
 
     def synchronize(self):
         check(lib.kamino_synchronize(self._h))
+
+    # ------------------------------------------------------- frame output
+    def frame_bytes(self, kind=FRAME_GRID):
+        n = ctypes.c_size_t()
+        check(lib.kamino_frame_bytes(self._h, kind, ctypes.byref(n)))
+        return n.value
+
+    def capture_frame(self, kind=FRAME_GRID):
+        """Queue a snapshot of the current state as a .bgeo frame; returns at
+        once (kamino_frame_capture)."""
+        check(lib.kamino_frame_capture(self._h, kind))
+
+    def write_frame(self, kind=FRAME_GRID, path=None):
+        """Oldest captured frame (or the current state) as .bgeo bytes; also
+        written to path when given (kamino_frame_write)."""
+        buf = ctypes.create_string_buffer(self.frame_bytes(kind))
+        check(lib.kamino_frame_write(self._h, kind, None if path is None else str(path).encode(), buf,
+                                     len(buf)))
+        return buf.raw
+
+    def write_data_bgeo(self, s, frame):
+        """KaminoSolver::write_data_bgeo: the grid frame to s + frame + ".bgeo"."""
+        check(lib.kamino_frame_write(self._h, FRAME_GRID, ("%s%d.bgeo" % (s, frame)).encode(), None, 0))
+
+    def write_particles_bgeo(self, s, frame):
+        """KaminoSolver::write_particles_bgeo: the particles to s + frame + ".bgeo"."""
+        check(lib.kamino_frame_write(self._h, FRAME_PARTICLES, ("%s%d.bgeo" % (s, frame)).encode(), None, 0))
+
+    def run_frames_bgeo(self, frames, grid_path=None, particle_path=None):
+        """Kamino::run with its .bgeo output (kamino_run_frames_bgeo)."""
+        n = ctypes.c_int64()
+        enc = lambda p: None if p is None else str(p).encode()
+        check(lib.kamino_run_frames_bgeo(self._h, frames, enc(grid_path), enc(particle_path), ctypes.byref(n)))
+        return n.value
+
+    def time_frame_pack(self, kind=FRAME_GRID, reps=10, flush_l2=True):
+        ms = ctypes.c_double()
+        check(lib.kamino_frame_time_pack(self._h, kind, reps, int(flush_l2), ctypes.byref(ms)))
+        return ms.value
 
     def time_elapsed(self):
         t, s = ctypes.c_double(), ctypes.c_int64()

@@ -836,3 +836,65 @@ void oracle_ref_init_fbm(int nt, float radius, float h, float *u, float *v)
         }
     }
 }
+
+/* ------------------------------------------------------------------------
+ * 3. Frame output records (oracle_frame_*), in the reference's host float
+ * arithmetic: KaminoSolver::write_data_bgeo (KaminoSolver.cu:284-357) and
+ * write_particles_bgeo (:359-396) with mapPToSphere / mapVToSphere
+ * (:398-423).  fReal is float; the vec3 components are double, so the
+ * cell-centre coordinates are exact double products rounded to float by
+ * the float locals of the map functions, and every other expression is a
+ * float expression (sinf / cosf are the float overloads the reference's
+ * sin / cos of a float resolve to).  Records are native-order floats:
+ * grid x y z 1 vx vy vz density (rows j, then columns i); particles
+ * x y z 1 0 0 0 r g b with zero colour (no colour image).
+ */
+void oracle_frame_grid(int nt, float radius, float h, const float *u, const float *v, const float *rho,
+                       float *rec)
+{
+    const int np = 2 * nt;
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < nt; ++j) {
+        for (int i = 0; i < np; ++i) {
+            const int ie = (i == np - 1) ? 0 : i + 1;
+            int jn, js;
+            if (j == 0) {
+                jn = js = 0;
+            } else if (j == nt - 1) {
+                jn = js = nt - 2;
+            } else {
+                jn = j - 1;
+                js = j;
+            }
+            const float uWest = u[(size_t)j * np + i], uEast = u[(size_t)j * np + ie];
+            const float vNorth = v[(size_t)jn * np + i], vSouth = v[(size_t)js * np + i];
+            const float velocityPhi = (float)((double)(uWest + uEast) / 2.0);
+            const float velocityTheta = (float)((double)(vNorth + vSouth) / 2.0);
+            const float phi = (float)(((double)i + 0.0) * (double)h);
+            const float theta = (float)(((double)j + 0.5) * (double)h);
+            float *r = rec + 8 * ((size_t)j * np + i);
+            r[4] = cosf(theta) * cosf(phi) * velocityTheta - sinf(phi) * velocityPhi;
+            r[6] = cosf(theta) * sinf(phi) * velocityTheta + cosf(phi) * velocityPhi;
+            r[5] = -sinf(theta) * velocityTheta;
+            r[0] = radius * sinf(theta) * cosf(phi);
+            r[2] = radius * sinf(theta) * sinf(phi);
+            r[1] = radius * cosf(theta);
+            r[3] = 1.0f;
+            r[7] = rho[(size_t)j * np + i];
+        }
+    }
+}
+
+void oracle_frame_particles(float radius, const float *part, int64_t n, float *rec)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < n; ++k) {
+        const float phi = part[2 * k], theta = part[2 * k + 1];
+        float *r = rec + 10 * k;
+        r[0] = radius * sinf(theta) * cosf(phi);
+        r[2] = radius * sinf(theta) * sinf(phi);
+        r[1] = radius * cosf(theta);
+        r[3] = 1.0f;
+        for (int c = 4; c < 10; ++c) r[c] = 0.0f;
+    }
+}

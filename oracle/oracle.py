@@ -53,6 +53,8 @@ def _oracle_lib():
         L.oracle_ref_index.argtypes = [_I, _P, _P, _I64, _F, _I, _P, _P]
         L.oracle_ref_wrap.argtypes = [_P, _P, _I64, _F, _P]
         L.oracle_ref_init_fbm.argtypes = [_I, _F, _F, _P, _P]
+        L.oracle_frame_grid.argtypes = [_I, _F, _F, _P, _P, _P, _P]
+        L.oracle_frame_particles.argtypes = [_F, _P, _I64, _P]
         _olib = L
     return _olib
 
@@ -145,6 +147,81 @@ class Oracle:
             v = np.ascontiguousarray(v, np.float32)
             self.L.oracle_divergence(self.o, u.ctypes.data, v.ctypes.data, out.ctypes.data)
         return out[: self.nt]
+
+
+# ------------------------------------------------------------ frame output
+# Partio's uncompressed BGEO layout (Houdini classic geometry), restated from
+# the format: big-endian int32 magic "Bgeo", char 'V', int32 version 5, eight
+# int32 counts (points, prims, point groups, prim groups, point attributes,
+# vertex attributes, prim attributes, detail attributes), one definition per
+# point attribute other than position (uint16 name length, name, uint16
+# size, int32 type: 0 float, 5 vector, size int32 defaults 0), the points
+# (x, y, z, w = 1, attribute values) and the trailer bytes 00 ff.  Partio
+# itself is not in the reference tree (only its headers); the layout is
+# anchored on the attribute lists of KaminoSolver.cu:290-293, 365-368.
+GRID_ATTRS = (("v", 3, 5), ("density", 1, 0))
+PARTICLE_ATTRS = (("v", 3, 5), ("color", 3, 5))
+
+
+def frame_grid_records(u, v, rho, nt, radius):
+    """write_data_bgeo's point records (KaminoSolver.cu:284-357): float32
+    [nt*np, 8] = x y z 1 vx vy vz density, rows j then columns i."""
+    L = _oracle_lib()
+    u = np.ascontiguousarray(u, np.float32)
+    v = np.ascontiguousarray(v, np.float32)
+    rho = np.ascontiguousarray(rho, np.float32)
+    rec = np.empty((nt * 2 * nt, 8), np.float32)
+    L.oracle_frame_grid(nt, float(np.float32(radius)), float(grid_h(nt)), u.ctypes.data, v.ctypes.data,
+                        rho.ctypes.data, rec.ctypes.data)
+    return rec
+
+
+def frame_particle_records(part, radius):
+    """write_particles_bgeo's point records (KaminoSolver.cu:359-396):
+    float32 [n, 10] = x y z 1 0 0 0 and a zero colour."""
+    L = _oracle_lib()
+    part = np.ascontiguousarray(part, np.float32).reshape(-1, 2)
+    rec = np.empty((part.shape[0], 10), np.float32)
+    if part.shape[0]:
+        L.oracle_frame_particles(float(np.float32(radius)), part.ctypes.data, part.shape[0], rec.ctypes.data)
+    return rec
+
+
+def bgeo_image(records, attrs):
+    """The .bgeo file bytes for float32 point records [n, 4 + sum(sizes)]."""
+    import struct
+    records = np.ascontiguousarray(records, np.float32)
+    out = [b"Bgeo", b"V", struct.pack(">i", 5),
+           struct.pack(">8i", records.shape[0], 0, 0, 0, len(attrs), 0, 0, 0)]
+    for name, size, typ in attrs:
+        out += [struct.pack(">H", len(name)), name.encode(), struct.pack(">Hi", size, typ),
+                struct.pack(">%di" % size, *([0] * size))]
+    out += [records.astype(">f4").tobytes(), b"\x00\xff"]
+    return b"".join(out)
+
+
+def read_bgeo(data):
+    """Parses a .bgeo image of the layout above: (attrs, records float32)."""
+    import struct
+    if data[:5] != b"BgeoV":
+        raise ValueError("not a BGEO V file")
+    (version,) = struct.unpack_from(">i", data, 5)
+    counts = struct.unpack_from(">8i", data, 9)
+    if version != 5 or any(counts[1:4]) or any(counts[5:]):
+        raise ValueError("unexpected header %r %r" % (version, counts))
+    off, attrs = 41, []
+    for _ in range(counts[4]):
+        (n,) = struct.unpack_from(">H", data, off)
+        name = data[off + 2:off + 2 + n].decode()
+        size, typ = struct.unpack_from(">Hi", data, off + 2 + n)
+        off += 2 + n + 6 + 4 * size
+        attrs.append((name, size, typ))
+    width = 4 + sum(a[1] for a in attrs)
+    end = off + 4 * width * counts[0]
+    if data[end:] != b"\x00\xff":
+        raise ValueError("bad trailer")
+    rec = np.frombuffer(data[off:end], ">f4").astype(np.float32).reshape(counts[0], width)
+    return tuple(attrs), rec
 
 
 def ref_index(kind, phi, theta, nt):

@@ -1,0 +1,90 @@
+"""Frame output (.bgeo) without a GPU: the oracle's restatement of
+write_data_bgeo / write_particles_bgeo (KaminoSolver.cu:284-423) against an
+independent FP64 numpy form of the same formulas, the file layout round
+trip, and argument errors at the C ABI."""
+import ctypes
+import struct
+
+import numpy as np
+
+
+def numpy_grid_records(u, v, rho, nt, radius):
+    """FP64 statement of write_data_bgeo's loop (KaminoSolver.cu:305-353)."""
+    npp = 2 * nt
+    h = np.float64(np.float32(np.pi / nt))
+    i = np.arange(npp)
+    j = np.arange(nt)
+    ue = np.roll(u, -1, axis=1)  # iEast = i + 1, wrapping at the seam
+    uphi = (u.astype(np.float64) + ue) / 2
+    jn = np.clip(j - 1, 0, nt - 2)
+    js = np.clip(j, 0, nt - 2)
+    jn[0] = js[0] = 0
+    uth = (v[jn].astype(np.float64) + v[js]) / 2
+    th = ((j + 0.5) * h)[:, None] * np.ones((1, npp))
+    ph = np.ones((nt, 1)) * (i * h)[None, :]
+    rec = np.empty((nt, npp, 8))
+    rec[..., 0] = radius * np.sin(th) * np.cos(ph)
+    rec[..., 1] = radius * np.cos(th)
+    rec[..., 2] = radius * np.sin(th) * np.sin(ph)
+    rec[..., 3] = 1.0
+    rec[..., 4] = np.cos(th) * np.cos(ph) * uth - np.sin(ph) * uphi
+    rec[..., 5] = -np.sin(th) * uth
+    rec[..., 6] = np.cos(th) * np.sin(ph) * uth + np.cos(ph) * uphi
+    rec[..., 7] = rho
+    return rec.reshape(-1, 8)
+
+
+def test_oracle_grid_records_follow_the_reference_formulas(orc):
+    nt, R = 64, 1.7
+    rng = np.random.default_rng(5)
+    u = rng.standard_normal((nt, 2 * nt)).astype(np.float32)
+    v = rng.standard_normal((nt - 1, 2 * nt)).astype(np.float32)
+    rho = (1 + 0.05 * rng.uniform(-1, 1, (nt, 2 * nt))).astype(np.float32)
+    got = orc.frame_grid_records(u, v, rho, nt, R)
+    want = numpy_grid_records(u, v, rho, nt, R)
+    assert np.array_equal(got[:, 3], np.ones(nt * 2 * nt, np.float32))
+    assert np.array_equal(got[:, 7], rho.reshape(-1))
+    assert np.abs(got[:, :3] - want[:, :3]).max() <= 4e-7 * R
+    assert np.abs(got[:, 4:7] - want[:, 4:7]).max() <= 4e-7 * np.abs(want[:, 4:7]).max()
+    # every point on the sphere; the centred velocity is tangent to it
+    assert np.abs(np.linalg.norm(got[:, :3].astype(np.float64), axis=1) - R).max() <= 4e-7 * R
+    radial = np.einsum("ij,ij->i", got[:, :3].astype(np.float64), got[:, 4:7]) / R
+    assert np.abs(radial).max() <= 1e-6 * np.abs(want[:, 4:7]).max()
+
+
+def test_oracle_particle_records(orc):
+    rng = np.random.default_rng(6)
+    n = 1000
+    part = np.stack([rng.uniform(0, 2 * np.pi, n), np.arccos(1 - 2 * rng.uniform(0, 1, n))], 1).astype(np.float32)
+    rec = orc.frame_particle_records(part, 2.0)
+    ph, th = part[:, 0].astype(np.float64), part[:, 1].astype(np.float64)
+    want = np.stack([2 * np.sin(th) * np.cos(ph), 2 * np.cos(th), 2 * np.sin(th) * np.sin(ph)], 1)
+    assert np.abs(rec[:, :3] - want).max() <= 1e-6
+    assert np.array_equal(rec[:, 3], np.ones(n, np.float32))
+    assert not rec[:, 4:].any()
+
+
+def test_bgeo_layout_round_trip(orc):
+    rec = np.arange(3 * 8, dtype=np.float32).reshape(3, 8)
+    img = orc.bgeo_image(rec, orc.GRID_ATTRS)
+    # header: magic, version, counts, then the two attribute definitions
+    assert img[:5] == b"BgeoV" and struct.unpack(">i", img[5:9]) == (5,)
+    assert struct.unpack(">8i", img[9:41]) == (3, 0, 0, 0, 2, 0, 0, 0)
+    assert img[41:44] == b"\x00\x01v" and struct.unpack(">Hi", img[44:50]) == (3, 5)
+    assert len(img) == 41 + (2 + 1 + 6 + 12) + (2 + 7 + 6 + 4) + 3 * 32 + 2
+    assert img[-2:] == b"\x00\xff"
+    attrs, back = orc.read_bgeo(img)
+    assert attrs == orc.GRID_ATTRS and np.array_equal(back, rec)
+    attrs, back = orc.read_bgeo(orc.bgeo_image(np.zeros((0, 10), np.float32), orc.PARTICLE_ATTRS))
+    assert attrs == orc.PARTICLE_ATTRS and back.shape == (0, 10)
+
+
+def test_frame_entry_points_reject_bad_arguments(kg):
+    n = ctypes.c_size_t()
+    assert kg.lib.kamino_frame_bytes(None, kg.FRAME_GRID, ctypes.byref(n)) == kg.ERR_INVALID
+    assert kg.lib.kamino_frame_bytes(None, 7, ctypes.byref(n)) == kg.ERR_INVALID
+    assert "kind" in kg._lib.last_error()
+    assert kg.lib.kamino_frame_capture(None, kg.FRAME_GRID) == kg.ERR_INVALID
+    assert kg.lib.kamino_frame_write(None, kg.FRAME_GRID, None, None, 0) == kg.ERR_INVALID
+    assert kg.lib.kamino_run_frames_bgeo(None, -1, None, None, None) == kg.ERR_INVALID
+    assert kg.lib.kamino_frame_time_pack(None, kg.FRAME_GRID, 0, 0, None) == kg.ERR_INVALID

@@ -1,0 +1,115 @@
+"""Frame output (.bgeo) on the GPU against the oracle.
+
+The device pack kernels build write_data_bgeo's and write_particles_bgeo's
+point records (KaminoSolver.cu:284-423) in the file's byte order.  Against
+the oracle's file image of the same state: header and trailer bytes equal,
+w and density bit-exact, positions and velocities within a few float ulps
+(only sinf / cosf differ between the device and the host C library).
+Capture order and the frame loop with output (Kamino::run, KaminoCore.cu:
+860-912) are checked bit for bit against frames written one by one.
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+POS_ULPS = 4e-7  # |device - host| of a coordinate, relative to the radius
+VEL_ULPS = 4e-7  # of a velocity component, relative to max |v|
+
+
+def make_solver(kg, nt, npart=0, seed=11, radius=1.0, frame_dt=None):
+    st = kg.make_initial_state(nt, lmax=8, seed=seed, n_particles=npart, radius=radius)
+    cfg = kg.default_config(n_theta=nt, radius=radius, dt=0.005, n_particles=npart)
+    if frame_dt is not None:
+        cfg.frame_dt = frame_dt
+    s = kg.KaminoSolver(config=cfg)
+    s.load(st)
+    return s
+
+
+def check_grid_image(orc, img, s, radius):
+    f = s.fields()
+    want_rec = orc.frame_grid_records(f["u_phi"], f["u_theta"], f["thickness"], s.nTheta, radius)
+    want = orc.bgeo_image(want_rec, orc.GRID_ATTRS)
+    assert len(img) == len(want) == s.frame_bytes()
+    attrs, rec = orc.read_bgeo(img)
+    nrec = rec.shape[0] * rec.shape[1] * 4
+    assert img[:len(img) - nrec - 2] == want[:len(want) - nrec - 2]  # header
+    assert img[-2:] == b"\x00\xff"
+    assert np.array_equal(rec[:, 3], want_rec[:, 3]) and np.array_equal(rec[:, 7], want_rec[:, 7])
+    assert np.abs(rec[:, :3] - want_rec[:, :3]).max() <= POS_ULPS * radius
+    vmax = np.abs(want_rec[:, 4:7]).max()
+    assert np.abs(rec[:, 4:7] - want_rec[:, 4:7]).max() <= VEL_ULPS * vmax
+
+
+@pytest.mark.parametrize("nt,radius", [(32, 1.0), (256, 1.5), (1024, 1.0), (2048, 1.0)])
+def test_grid_frame_matches_oracle(kg, orc, nt, radius):
+    with make_solver(kg, nt, radius=radius) as s:
+        s.step_n(3)
+        img = s.write_frame(kg.FRAME_GRID)
+        check_grid_image(orc, img, s, radius)
+
+
+def test_particle_frame_matches_oracle(kg, orc):
+    nt, npart = 128, 4096
+    with make_solver(kg, nt, npart=npart, radius=2.0) as s:
+        s.step_n(5)
+        img = s.write_frame(kg.FRAME_PARTICLES)
+        part = s.get_state(kg.PARTICLES)
+    want_rec = orc.frame_particle_records(part, 2.0)
+    want = orc.bgeo_image(want_rec, orc.PARTICLE_ATTRS)
+    assert len(img) == len(want)
+    attrs, rec = orc.read_bgeo(img)
+    assert attrs == orc.PARTICLE_ATTRS
+    assert img[:len(img) - rec.nbytes - 2] == want[:len(want) - rec.nbytes - 2]
+    assert np.array_equal(rec[:, 3:], want_rec[:, 3:])
+    assert np.abs(rec[:, :3] - want_rec[:, :3]).max() <= POS_ULPS * 2.0
+
+
+def test_captures_are_written_oldest_first(kg, orc):
+    with make_solver(kg, 64) as s:
+        s.capture_frame()
+        before = s.fields()
+        s.step_n(2)
+        s.capture_frame()
+        with pytest.raises(kg.KaminoError):  # two wait already
+            s.capture_frame()
+        first = s.write_frame()
+        second = s.write_frame()
+        now = s.write_frame()  # nothing waits: the current state
+    assert second == now and first != second
+    _, rec = orc.read_bgeo(first)
+    assert np.array_equal(rec[:, 7], before["thickness"].reshape(-1))
+
+
+def test_run_frames_bgeo_writes_every_frame(kg, orc, tmp_path):
+    nt, frames, frame_dt = 64, 3, 0.012  # 0.012 / 0.005: 3 steps per frame
+    with make_solver(kg, nt, npart=512, frame_dt=frame_dt) as s:
+        steps = s.run_frames_bgeo(frames, str(tmp_path / "grid_"), str(tmp_path / "part_"))
+        last = s.write_frame(kg.FRAME_GRID)
+    assert steps == kg.frame_steps(0.005, frame_dt, frames)
+    names = sorted(os.listdir(tmp_path))
+    assert names == sorted(["grid_%d.bgeo" % i for i in range(frames + 1)] +
+                           ["part_%d.bgeo" % i for i in range(frames + 1)])
+    # the same frames written one at a time, with the frame loop's step counts
+    per_frame = [kg.frame_steps(0.005, frame_dt, i) - kg.frame_steps(0.005, frame_dt, i - 1)
+                 for i in range(1, frames + 1)]
+    with make_solver(kg, nt, npart=512, frame_dt=frame_dt) as s:
+        ref = {0: (s.write_frame(kg.FRAME_GRID), s.write_frame(kg.FRAME_PARTICLES))}
+        for i, n in enumerate(per_frame, 1):
+            s.step_n(n)
+            ref[i] = (s.write_frame(kg.FRAME_GRID), s.write_frame(kg.FRAME_PARTICLES))
+        check_grid_image(orc, ref[frames][0], s, 1.0)
+    for i in range(frames + 1):
+        assert (tmp_path / ("grid_%d.bgeo" % i)).read_bytes() == ref[i][0], i
+        assert (tmp_path / ("part_%d.bgeo" % i)).read_bytes() == ref[i][1], i
+    assert last == ref[frames][0]
+
+
+def test_frame_write_reports_io_errors(kg, tmp_path):
+    with make_solver(kg, 32) as s:
+        with pytest.raises(kg.KaminoError) as e:
+            s.write_frame(kg.FRAME_GRID, path=tmp_path / "missing_dir" / "f.bgeo")
+        assert e.value.code == kg._lib.ERR_IO and "cannot open" in str(e.value)
