@@ -24,7 +24,7 @@
  *    bytes, exactly like KaminoQuantity::copyToGPU/copyBackToCPU
  *    (KaminoQuantity.cu:3-18).  u_phi and thickness have nTheta rows,
  *    u_theta has nTheta-1 rows, nPhi = 2*nTheta columns.  Particles are
- *    interleaved (phi, theta) float pairs (KaminoParticles.cu:28-30).
+ *    interleaved (phi, theta) float pairs (KaminoParticles.cu:61-62).
  *  - nTheta must be a power of two in [32, 2048]; the reference's cyclic
  *    reduction has the same power-of-two rule (tdm.cu:11-13).
  */
@@ -102,7 +102,7 @@ typedef struct kamino_config {
     char color_image[256];    /*                                 main.cu:41-45 */
     /* extensions */
     int64_t n_particles;      /* <0: count from particle_density as
-                                 KaminoParticles.cu:194-200 does          */
+                                 KaminoParticles.cu:20-26 does          */
     uint32_t flags;           /* kamino_flags                              */
     int32_t fp64_modes;       /* Fourier modes |m| <= this are solved in
                                  FP64 (default 4; 0 = all FP32)            */
@@ -121,7 +121,9 @@ int kamino_config_default(kamino_config* cfg);
 int kamino_parse_config(const char* path, kamino_config* cfg);
 
 /* Number of particles the reference would create for a config
- * (KaminoParticles.cu:194-200): 2 * floor(sqrt(d) * nTheta)^2. */
+ * (KaminoParticles.cu:20-26): 2 * floor(sqrt(d) * nTheta)^2, with d the
+ * particle density truncated to an integer (Kamino::run passes it through
+ * initParticlesfromPic's size_t parameter, KaminoSolver.cu:278). */
 int64_t kamino_particle_count(const kamino_config* cfg);
 
 /* Steps the frame loop of Kamino::run takes (KaminoCore.cu:886-895); -1 on
@@ -146,6 +148,18 @@ int kamino_destroy(kamino_handle h);
  * pitch_bytes is the host row pitch (ignored for particles).  Synchronous. */
 int kamino_set_state(kamino_handle h, int field, const float* host, size_t pitch_bytes);
 int kamino_get_state(kamino_handle h, int field, float* host, size_t pitch_bytes);
+
+/* The reference's particle placement, KaminoParticles::KaminoParticles
+ * without a colour image (KaminoParticles.cu:20-62; reached through
+ * KaminoSolver::initParticlesfromPic, KaminoSolver.cu:278-281): a jittered
+ * grid of 2 floor(sqrt(d) nTheta)^2 particles drawn with the C library's
+ * rand() sequence after srand(seed) (the reference never seeds: seed 1), in
+ * its float arithmetic.  kamino_reference_particles fills n (phi, theta)
+ * pairs on the host (n must be that count for cfg->particle_density and
+ * cfg->n_theta; the caller's rand() state is not touched);
+ * kamino_init_particles uploads them to a handle created with that count. */
+int kamino_reference_particles(const kamino_config* cfg, uint32_t seed, float* out, int64_t n);
+int kamino_init_particles(kamino_handle h, uint32_t seed);
 
 /* Replaces KaminoSolver::initialize_velocity (KaminoInitializer.cu:3-85),
  * which the reference's constructor runs (KaminoSolver.cu:59): sets u_phi

@@ -119,6 +119,8 @@ SIGNATURES = {
     "kamino_step": (_I, [_P, _F]),
     "kamino_step_host": (_I, [_P, _F, _P, _P, _P, _P, _P, _P, _SZ]),
     "kamino_init_fbm": (_I, [_P]),
+    "kamino_reference_particles": (_I, [ctypes.POINTER(KaminoConfig), ctypes.c_uint32, _P, _I64]),
+    "kamino_init_particles": (_I, [_P, ctypes.c_uint32]),
     "kamino_advection": (_I, [_P]),
     "kamino_geometric": (_I, [_P]),
     "kamino_projection": (_I, [_P]),

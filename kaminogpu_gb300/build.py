@@ -1,4 +1,5 @@
-"""Builds libkamino_gb300.so in-tree (kaminogpu_gb300/lib/) with nvcc for sm_103a.
+"""Builds libkamino_gb300.so in-tree (kaminogpu_gb300/lib/) with nvcc for sm_103a,
+and the `kamino` executable (kamino configKamino.txt) linked against it.
 
 Translation units compile in parallel; the shared library links against the
 shared CUDA runtime.  Re-running is cheap: a unit is rebuilt only when a
@@ -13,6 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "lib")
 LIB = os.path.join(OUT, "libkamino_gb300.so")
+CLI = os.path.join(OUT, "kamino")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -53,15 +55,30 @@ def build(verbose=False):
     units = [u for u in UNITS if os.path.exists(os.path.join(CSRC, u))]
     with ThreadPoolExecutor(max_workers=len(units)) as ex:
         objs = list(ex.map(lambda u: _compile(u, hdr, verbose), units))
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
-        return LIB
-    cmd = [NVCC, *ARCH, "-shared", "--cudart", "shared", "-o", LIB, *objs,
-           "-Xcompiler", "-fopenmp", "-L" + os.path.join(CUDA, "lib64"),
-           "-Xlinker", "-rpath," + os.path.join(CUDA, "lib64")]
+    if not (os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs)):
+        cmd = [NVCC, *ARCH, "-shared", "--cudart", "shared", "-o", LIB, *objs,
+               "-Xcompiler", "-fopenmp", "-L" + os.path.join(CUDA, "lib64"),
+               "-Xlinker", "-rpath," + os.path.join(CUDA, "lib64")]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    _build_cli()
+    return LIB
+
+
+def _build_cli():
+    """The `kamino` executable (csrc/kamino_main.cpp) over the C ABI."""
+    src = os.path.join(CSRC, "kamino_main.cpp")
+    if not os.path.exists(src):
+        return None
+    if os.path.exists(CLI) and os.path.getmtime(CLI) >= max(os.path.getmtime(src), os.path.getmtime(LIB)):
+        return CLI
+    cmd = ["g++", "-O2", "-std=c++17", "-I" + os.path.join(HERE, "..", "include"), src, "-o", CLI,
+           "-L" + OUT, "-lkamino_gb300", "-Wl,-rpath,$ORIGIN"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError("link failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
-    return LIB
+        raise RuntimeError("CLI build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return CLI
 
 
 if __name__ == "__main__":

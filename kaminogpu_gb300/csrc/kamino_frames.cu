@@ -28,15 +28,12 @@
 //   trailer bytes 0x00, 0xff.
 // Grid records: position(3) w v(3) density(1) = 32 bytes; particle records:
 // position(3) w v(3) color(3) = 40 bytes.
-#include <algorithm>
-#include <atomic>
 #include <cerrno>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <string>
-#include <thread>
 #include <vector>
 
 #include <fcntl.h>
@@ -112,7 +109,7 @@ __global__ void __launch_bounds__(FRAME_THREADS) k_frame_grid(KGeo g, const floa
 // One thread per particle: mapPToSphere of (phi, theta) (KaminoSolver.cu:
 // 373-393), velocity 0, colour 0.  The colours come from the reference's
 // image input (initParticlesfromPic), which is not built; without an image
-// the reference's colours are zero too (KaminoParticles.cu:68-73).
+// the reference's colours are zero too (KaminoParticles.cu:73-78).
 __global__ void __launch_bounds__(FRAME_THREADS) k_frame_particles(float R, const float2* __restrict__ part,
                                                                    int64_t n, uint2* __restrict__ out)
 {
@@ -318,38 +315,26 @@ int capture(kamino_handle h, KFrames* f, int kind)
     return KAMINO_OK;
 }
 
-// Writes n bytes to path.  Large files are written by several threads with
-// pwrite at disjoint offsets: one thread's copy into the page cache runs at a
-// few GB/s, well below what the host's memory system sustains.
+// Writes n bytes to path.  (Writing with several threads at disjoint
+// offsets was measured: buffered writes to one file take the inode's lock,
+// so it gained nothing.)
 int write_file(const char* path, const uint8_t* data, size_t n)
 {
     const int fd = ::open(path, O_WRONLY | O_CREAT | O_TRUNC, 0644);
     if (fd < 0) return kamino_fail(KAMINO_ERR_IO, "cannot open %s for writing: %s", path, std::strerror(errno));
-    constexpr size_t CHUNK_MIN = (size_t)8 << 20;
-    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    const int nthreads = (int)std::min<size_t>({8, (size_t)hw, std::max<size_t>(1, n / CHUNK_MIN)});
-    std::atomic<int> failed{0};
-    auto part = [&](int t) {
-        size_t lo = n * t / nthreads;
-        const size_t hi = n * (t + 1) / nthreads;
-        while (lo < hi) {
-            const ssize_t w = ::pwrite(fd, data + lo, hi - lo, (off_t)lo);
-            if (w < 0 && errno == EINTR) continue;
-            if (w <= 0) {
-                failed.store(w < 0 ? errno : EIO);
-                return;
-            }
-            lo += (size_t)w;
+    size_t done = 0;
+    int err = 0;
+    while (done < n) {
+        const ssize_t w = ::write(fd, data + done, n - done);
+        if (w < 0 && errno == EINTR) continue;
+        if (w <= 0) {
+            err = w < 0 ? errno : EIO;
+            break;
         }
-    };
-    std::vector<std::thread> pool;
-    for (int t = 1; t < nthreads; t++) pool.emplace_back(part, t);
-    part(0);
-    for (auto& th : pool) th.join();
-    const int c = ::close(fd);
-    if (failed.load() || c != 0)
-        return kamino_fail(KAMINO_ERR_IO, "write to %s failed: %s", path,
-                           std::strerror(failed.load() ? failed.load() : errno));
+        done += (size_t)w;
+    }
+    if (::close(fd) != 0 && !err) err = errno;
+    if (err) return kamino_fail(KAMINO_ERR_IO, "write to %s failed: %s", path, std::strerror(err));
     return KAMINO_OK;
 }
 

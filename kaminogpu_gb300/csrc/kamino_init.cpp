@@ -1,16 +1,18 @@
 // kamino_init.cpp — host side of the C ABI that needs no GPU: config
 // defaults and parsing (KaminoGPU/kernel/main.cu:17-45), the particle count
-// rule (KaminoParticles.cu:194-200) and the seeded synthetic initial states.
+// rule (KaminoParticles.cu:20-26) and the seeded synthetic initial states.
 //
 // The reference initialises velocity from FBM curl noise
 // (KaminoInitializer.cu:3-134), thickness from an image and particles from a
-// jittered grid with unseeded rand() (KaminoParticles.cu:33-80).  The
-// workloads here are seeded instead: a spherical-harmonic stream function
+// jittered grid with unseeded rand() (KaminoParticles.cu:33-62); the last is
+// kamino_reference_particles below.  The benchmark workloads are seeded
+// instead: a spherical-harmonic stream function
 // (plus an optional Gaussian vortex), thickness 1 + a*U(-1,1), particles
 // uniform on the sphere.  Every draw comes from a splitmix64-seeded
 // xoshiro256** stream, so the same seed gives the same state on any host.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <string>
@@ -162,16 +164,84 @@ extern "C" int kamino_parse_config(const char* path, kamino_config* cfg)
     return KAMINO_OK;
 }
 
+// The particle density as KaminoParticles receives it: the config's fReal
+// value truncated to size_t by initParticlesfromPic, then back to fReal.
+static float reference_density(double d)
+{
+    const float f = (float)d;
+    return f > 0.0f ? (float)(size_t)f : 0.0f;
+}
+
 extern "C" int64_t kamino_particle_count(const kamino_config* cfg)
 {
     if (!cfg) return -1;
     if (cfg->n_particles >= 0) return cfg->n_particles;
-    // KaminoParticles.cu:194-200: linearDensity = sqrt(particleDensity) in
-    // fReal; numTheta = (unsigned)(linearDensity * nTheta); numPhi = 2*numTheta
-    float linearDensity = std::sqrt((float)cfg->particle_density);
+    // KaminoParticles.cu:20-26: linearDensity = sqrt(particleDensity) in
+    // fReal; numTheta = (unsigned)(linearDensity * nTheta); numPhi = 2*numTheta.
+    // The density reaches it through initParticlesfromPic's size_t parameter
+    // (KaminoSolver.cu:278, called with the fReal density at KaminoCore.cu:865),
+    // so its fraction is dropped first.
+    float linearDensity = std::sqrt(reference_density(cfg->particle_density));
     unsigned numThetaParticles = (unsigned)(linearDensity * (float)(size_t)cfg->n_theta);
     unsigned numPhiParticles = 2 * numThetaParticles;
     return (int64_t)numThetaParticles * (int64_t)numPhiParticles;
+}
+
+// KaminoParticles::KaminoParticles (KaminoParticles.cu:20-62): a jittered
+// grid of numPhi x numTheta particles, four rand() draws per particle (two
+// signs, two offsets of up to half a spacing), in the reference's float
+// arithmetic, particle index i * numTheta + j.  The draws come from the C
+// library's random() generator seeded like srand(seed) (the reference never
+// seeds it: seed 1), through the reentrant random_r so the caller's own
+// rand() sequence is left alone; with the GNU C library that is the sequence
+// the reference's rand() gives.
+extern "C" int kamino_reference_particles(const kamino_config* cfg, uint32_t seed, float* out, int64_t n)
+{
+    if (!cfg || !out) return kamino_fail(KAMINO_ERR_INVALID, "kamino_reference_particles: null argument");
+    kamino_config c = *cfg;
+    c.n_particles = -1;
+    const int64_t want = kamino_particle_count(&c);
+    if (n != want)
+        return kamino_fail(KAMINO_ERR_INVALID, "particle_density %g at nTheta %d makes %lld particles, not %lld",
+                           cfg->particle_density, cfg->n_theta, (long long)want, (long long)n);
+    const float linearDensity = std::sqrt(reference_density(cfg->particle_density));
+    const size_t nTheta = (size_t)cfg->n_theta;
+    const float delta = (float)(KAMINO_PI_D / (double)nTheta / (double)linearDensity);
+    const float halfDelta = (float)((double)delta / 2.0);
+    const unsigned numThetaParticles = (unsigned)(linearDensity * (float)nTheta);
+    const unsigned numPhiParticles = 2 * numThetaParticles;
+    char state[128];
+    struct random_data rd;
+    std::memset(&rd, 0, sizeof(rd));
+    std::memset(state, 0, sizeof(state));
+    if (initstate_r(seed, state, sizeof(state), &rd) != 0)
+        return kamino_fail(KAMINO_ERR_INVALID, "initstate_r failed");
+    auto draw = [&rd]() {
+        int32_t r = 0;
+        random_r(&rd, &r);
+        return (float)r / (float)RAND_MAX;
+    };
+    for (unsigned i = 0; i < numPhiParticles; ++i) {
+        for (unsigned j = 0; j < numThetaParticles; ++j) {
+            float signPhi = draw();
+            signPhi = signPhi >= 0.5f ? 1.0f : -1.0f;
+            float signTheta = draw();
+            signTheta = signTheta >= 0.5f ? 1.0f : -1.0f;
+            int32_t r = 0;
+            random_r(&rd, &r);
+            const float randPhi = signPhi * halfDelta * (float)r / (float)RAND_MAX;
+            random_r(&rd, &r);
+            const float randTheta = signTheta * halfDelta * (float)r / (float)RAND_MAX;
+            float phi = (float)i * delta + randPhi;
+            float theta = (float)j * delta + randTheta;
+            if (phi < 0.0f) phi = 0.0f;
+            if (theta < 0.0f) theta = 0.0f;
+            const size_t index = (size_t)i * numThetaParticles + j;
+            out[2 * index] = phi;
+            out[2 * index + 1] = theta;
+        }
+    }
+    return KAMINO_OK;
 }
 
 extern "C" int kamino_init_spec_default(kamino_init_spec* spec)
@@ -345,4 +415,18 @@ extern "C" int kamino_abi_sizes(size_t* out, int n)
     if (!out) return KAMINO_ERR_INVALID;
     for (int i = 0; i < n && i < 4; i++) out[i] = s[i];
     return KAMINO_OK;
+}
+
+// KaminoSolver::initParticlesfromPic without an image (KaminoSolver.cu:
+// 278-281): the reference's particle placement, uploaded to the handle.
+extern "C" int kamino_init_particles(kamino_handle h, uint32_t seed)
+{
+    kamino_config cfg;
+    int rc = kamino_internal_config(h, &cfg);
+    if (rc) return rc;
+    const int64_t n = kamino_particle_count(&cfg);
+    if (n == 0) return KAMINO_OK;
+    std::vector<float> buf(2 * (size_t)n);
+    if ((rc = kamino_reference_particles(&cfg, seed, buf.data(), n))) return rc;
+    return kamino_set_state(h, KAMINO_PARTICLES, buf.data(), 0);
 }

@@ -147,6 +147,13 @@ class KaminoSolver:
         """The reference's FBM curl-noise velocity (kamino_init_fbm)."""
         check(lib.kamino_init_fbm(self._h))
 
+    def initParticlesfromPic(self, path="", seed=1):
+        """KaminoSolver::initParticlesfromPic without an image: the reference's
+        jittered particle placement (kamino_init_particles)."""
+        if path:
+            raise ValueError("image input is not supported")
+        check(lib.kamino_init_particles(self._h, seed))
+
     def step_host(self, u_phi, u_theta, thickness, dt=None):
         """One step with the state in host memory (kamino_step_host): uploads
         the three fields, steps, and returns the new three as arrays."""

@@ -898,3 +898,36 @@ void oracle_frame_particles(float radius, const float *part, int64_t n, float *r
         for (int c = 4; c < 10; ++c) r[c] = 0.0f;
     }
 }
+
+/* KaminoParticles::KaminoParticles (KaminoParticles.cu:20-62) without a
+ * colour image: the jittered particle grid, drawn with the C library's
+ * srand(seed) / rand() as the reference does (it never seeds: seed 1), in its
+ * float arithmetic (fReal variables, double literals M_PI, 0.5, 2.0, 0.0).
+ * out: (phi, theta) pairs, index i * numTheta + j.  Returns the count. */
+int64_t oracle_ref_particles(float particleDensity, int nTheta, unsigned seed, float *out)
+{
+    const float linearDensity = sqrtf(particleDensity);
+    const float delta = (float)(3.14159265358979323846 / (double)(size_t)nTheta / (double)linearDensity);
+    const float halfDelta = (float)((double)delta / 2.0);
+    const unsigned numThetaParticles = (unsigned)(linearDensity * (float)(size_t)nTheta);
+    const unsigned numPhiParticles = 2 * numThetaParticles;
+    srand(seed);
+    for (unsigned i = 0; i < numPhiParticles; ++i) {
+        for (unsigned j = 0; j < numThetaParticles; ++j) {
+            float signPhi = (float)rand() / (float)RAND_MAX;
+            signPhi = (double)signPhi >= 0.5 ? 1.0f : -1.0f;
+            float signTheta = (float)rand() / (float)RAND_MAX;
+            signTheta = (double)signTheta >= 0.5 ? 1.0f : -1.0f;
+            float randPhi = signPhi * halfDelta * (float)rand() / (float)RAND_MAX;
+            float randTheta = signTheta * halfDelta * (float)rand() / (float)RAND_MAX;
+            float phi = (float)i * delta + randPhi;
+            float theta = (float)j * delta + randTheta;
+            if ((double)phi < 0.0) phi = 0.0f;
+            if ((double)theta < 0.0) theta = 0.0f;
+            size_t index = (size_t)i * numThetaParticles + j;
+            out[2 * index] = phi;
+            out[2 * index + 1] = theta;
+        }
+    }
+    return (int64_t)numThetaParticles * numPhiParticles;
+}

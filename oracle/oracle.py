@@ -55,6 +55,8 @@ def _oracle_lib():
         L.oracle_ref_init_fbm.argtypes = [_I, _F, _F, _P, _P]
         L.oracle_frame_grid.argtypes = [_I, _F, _F, _P, _P, _P, _P]
         L.oracle_frame_particles.argtypes = [_F, _P, _I64, _P]
+        L.oracle_ref_particles.argtypes = [_F, _I, ctypes.c_uint, _P]
+        L.oracle_ref_particles.restype = _I64
         _olib = L
     return _olib
 
@@ -185,6 +187,21 @@ def frame_particle_records(part, radius):
     if part.shape[0]:
         L.oracle_frame_particles(float(np.float32(radius)), part.ctypes.data, part.shape[0], rec.ctypes.data)
     return rec
+
+
+def ref_particles(particle_density, nt, seed=1):
+    """KaminoParticles' jittered grid (KaminoParticles.cu:20-62) drawn with
+    srand(seed) / rand(): float32 [n, 2] (phi, theta)."""
+    L = _oracle_lib()
+    # Kamino::run hands the density to KaminoParticles through a size_t
+    # parameter (KaminoSolver.cu:278): the fraction is dropped
+    d = np.float32(int(np.float32(particle_density)))
+    lin = np.sqrt(d)
+    n_theta = int(np.float32(lin * np.float32(nt)))
+    out = np.empty((2 * n_theta * n_theta, 2), np.float32)
+    n = L.oracle_ref_particles(float(d), nt, seed, out.ctypes.data)
+    assert n == out.shape[0]
+    return out
 
 
 def bgeo_image(records, attrs):

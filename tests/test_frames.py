@@ -6,6 +6,7 @@ import ctypes
 import struct
 
 import numpy as np
+import pytest
 
 
 def numpy_grid_records(u, v, rho, nt, radius):
@@ -88,3 +89,39 @@ def test_frame_entry_points_reject_bad_arguments(kg):
     assert kg.lib.kamino_frame_write(None, kg.FRAME_GRID, None, None, 0) == kg.ERR_INVALID
     assert kg.lib.kamino_run_frames_bgeo(None, -1, None, None, None) == kg.ERR_INVALID
     assert kg.lib.kamino_frame_time_pack(None, kg.FRAME_GRID, 0, 0, None) == kg.ERR_INVALID
+
+
+@pytest.mark.parametrize("density,nt,seed", [(1.0, 32, 1), (4.0, 64, 1), (2.0, 64, 7), (3.7, 32, 1)])
+def test_reference_particles_match_the_rand_restatement(kg, orc, density, nt, seed):
+    """KaminoParticles' jittered grid (KaminoParticles.cu:20-62): the library's
+    placement (reentrant random_r) equals the oracle's srand/rand restatement
+    bit for bit, and leaves the caller's rand() sequence alone."""
+    libc = ctypes.CDLL(None)
+    cfg = kg.default_config(n_theta=nt, particle_density=density, n_particles=-1)
+    n = kg.particle_count(cfg)
+    want = orc.ref_particles(density, nt, seed)
+    assert want.shape == (n, 2)
+    libc.srand(5)
+    first = libc.rand()
+    libc.srand(5)
+    got = np.empty((n, 2), np.float32)
+    kg.check(kg.lib.kamino_reference_particles(ctypes.byref(cfg), seed, got.ctypes.data, n))
+    assert libc.rand() == first
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    h = np.float32(np.pi / nt)
+    assert got.min() >= 0 and got[:, 1].max() < np.pi + h and got[:, 0].max() < 2 * np.pi + h
+    assert kg.lib.kamino_reference_particles(ctypes.byref(cfg), seed, got.ctypes.data, n + 1) == kg.ERR_INVALID
+
+
+def test_cli_usage_and_config_errors(kg, tmp_path):
+    import os
+    import subprocess
+    exe = os.path.join(os.path.dirname(kg.LIB_PATH), "kamino")
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 255 and "configKamino.txt" in r.stdout
+    r = subprocess.run([exe, str(tmp_path / "missing.txt")], capture_output=True, text=True)
+    assert r.returncode == 1 and "cannot open config file" in r.stderr
+    bad = tmp_path / "bad.txt"
+    bad.write_text("1.0 32 1.0\n")
+    r = subprocess.run([exe, str(bad)], capture_output=True, text=True)
+    assert r.returncode == 1 and "16 whitespace-separated fields" in r.stderr

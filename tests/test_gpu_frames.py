@@ -113,3 +113,40 @@ def test_frame_write_reports_io_errors(kg, tmp_path):
         with pytest.raises(kg.KaminoError) as e:
             s.write_frame(kg.FRAME_GRID, path=tmp_path / "missing_dir" / "f.bgeo")
         assert e.value.code == kg._lib.ERR_IO and "cannot open" in str(e.value)
+
+
+def test_init_particles_uploads_the_reference_placement(kg, orc):
+    cfg = kg.default_config(n_theta=64, radius=1.0, dt=0.005, particle_density=2.0, n_particles=-1)
+    with kg.KaminoSolver(config=cfg) as s:
+        kg.check(kg.lib.kamino_init_particles(s._h, 1))
+        got = s.get_state(kg.PARTICLES)
+    assert np.array_equal(got.view(np.uint32), orc.ref_particles(2.0, 64, 1).view(np.uint32))
+
+
+def test_cli_runs_the_reference_frame_loop(kg, orc, tmp_path):
+    """`kamino configKamino.txt` (main.cu:4-59, Kamino::run): the files it
+    writes equal the library's own frame loop on the same start (FBM velocity,
+    the reference's particle placement), bit for bit."""
+    import subprocess
+    nt, dens, dt, DT, frames = 32, 1.0, 0.005, 0.012, 3
+    cfgfile = tmp_path / "configKamino.txt"
+    cfgfile.write_text("1.0\n%d\n%g\n%g\n%g\n%d\n0.0 1 1 1 1\n%s\n%s\nnull\nnull\nnull\n"
+                       % (nt, dens, dt, DT, frames, tmp_path / "cli_grid_", tmp_path / "cli_part_"))
+    exe = os.path.join(os.path.dirname(kg.LIB_PATH), "kamino")
+    r = subprocess.run([exe, str(cfgfile)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert "Frame %d is ready" % frames in r.stdout and "Performance:" in r.stdout
+    cfg = kg.parse_config(cfgfile)
+    with kg.KaminoSolver(config=cfg) as s:
+        s.init_fbm()
+        kg.check(kg.lib.kamino_init_particles(s._h, 1))
+        part0 = s.get_state(kg.PARTICLES)
+        s.run_frames_bgeo(frames, str(tmp_path / "lib_grid_"), str(tmp_path / "lib_part_"))
+    for i in range(frames + 1):
+        for k in ("grid", "part"):
+            a = (tmp_path / ("cli_%s_%d.bgeo" % (k, i))).read_bytes()
+            assert a == (tmp_path / ("lib_%s_%d.bgeo" % (k, i))).read_bytes(), (k, i)
+    _, rec = orc.read_bgeo((tmp_path / "cli_part_0.bgeo").read_bytes())
+    want = orc.frame_particle_records(part0, 1.0)
+    assert rec.shape[0] == kg.particle_count(cfg) == 2 * 32 * 32
+    assert np.abs(rec[:, :3] - want[:, :3]).max() <= POS_ULPS
