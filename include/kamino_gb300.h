@@ -161,6 +161,24 @@ int kamino_get_state(kamino_handle h, int field, float* host, size_t pitch_bytes
 int kamino_reference_particles(const kamino_config* cfg, uint32_t seed, float* out, int64_t n);
 int kamino_init_particles(kamino_handle h, uint32_t seed);
 
+/* Image inputs with the image decoded by the caller (the reference reads it
+ * with OpenCV's imread, which is not part of this library): 8-bit pixels in
+ * OpenCV's B, G, R order, width x height, row stride in bytes.  As the
+ * reference, the image is mirrored left-right (cv::flip code 1) and
+ * resampled to nPhi x nTheta pixels (cv::resize, INTER_LINEAR): here on the
+ * device, bilinear at half-pixel centres with the edges clamped, each
+ * channel rounded to 8 bits.
+ *   kamino_init_density_image replaces KaminoSolver::initDensityfromPic
+ *   (KaminoSolver.cu:243-277): thickness(i, j) = (B + G + R) / 3 of pixel
+ *   (i, j), each channel / 255.
+ *   kamino_init_particle_colors_image gives the particles, as placed now,
+ *   the colours KaminoParticles takes from its image (KaminoParticles.cu:
+ *   6-17, 56-72): (G, R, B) / 255 of the pixel of the particle's cell; they
+ *   appear in the particle .bgeo files. */
+int kamino_init_density_image(kamino_handle h, const uint8_t* bgr, int width, int height, size_t stride);
+int kamino_init_particle_colors_image(kamino_handle h, const uint8_t* bgr, int width, int height,
+                                      size_t stride);
+
 /* Replaces KaminoSolver::initialize_velocity (KaminoInitializer.cu:3-85),
  * which the reference's constructor runs (KaminoSolver.cu:59): sets u_phi
  * and u_theta to the reference's FBM curl-noise velocity, evaluated on the
@@ -231,8 +249,10 @@ int kamino_run_frames(kamino_handle h, int frames, int64_t* steps_taken);
  *                           and density (the thickness);
  *   KAMINO_FRAME_PARTICLES  KaminoSolver::write_particles_bgeo (:359-396):
  *                           one point per particle, position, v = 0 and
- *                           color (0: the reference's colours come from its
- *                           image input, which is not built).
+ *                           color as the reference writes it (components
+ *                           3i+1..3i+3 of its per-particle (G, R, B) array,
+ *                           :375-377; zero without a colour image, see
+ *                           kamino_init_particle_colors_image).
  * The records are computed on the device in the file's byte order and
  * copied to pinned host memory on a second stream, so work issued after a
  * capture overlaps the copy. */

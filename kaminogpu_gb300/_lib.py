@@ -121,6 +121,8 @@ SIGNATURES = {
     "kamino_init_fbm": (_I, [_P]),
     "kamino_reference_particles": (_I, [ctypes.POINTER(KaminoConfig), ctypes.c_uint32, _P, _I64]),
     "kamino_init_particles": (_I, [_P, ctypes.c_uint32]),
+    "kamino_init_density_image": (_I, [_P, _P, _I, _I, _SZ]),
+    "kamino_init_particle_colors_image": (_I, [_P, _P, _I, _I, _SZ]),
     "kamino_advection": (_I, [_P]),
     "kamino_geometric": (_I, [_P]),
     "kamino_projection": (_I, [_P]),

@@ -1,5 +1,6 @@
-// kamino_frames.cu — frame output: the .bgeo files Kamino writes after every
-// frame, built on the device.
+// kamino_frames.cu — frame I/O: the .bgeo files Kamino writes after every
+// frame, built on the device, and the image inputs (thickness and particle
+// colours from a decoded image), resampled on the device.
 //
 // The reference writes two files per frame through Partio
 // (KaminoSolver::write_data_bgeo / write_particles_bgeo, KaminoSolver.cu:
@@ -28,6 +29,7 @@
 //   trailer bytes 0x00, 0xff.
 // Grid records: position(3) w v(3) density(1) = 32 bytes; particle records:
 // position(3) w v(3) color(3) = 40 bytes.
+#include <algorithm>
 #include <cerrno>
 #include <cmath>
 #include <cstdint>
@@ -107,11 +109,14 @@ __global__ void __launch_bounds__(FRAME_THREADS) k_frame_grid(KGeo g, const floa
 }
 
 // One thread per particle: mapPToSphere of (phi, theta) (KaminoSolver.cu:
-// 373-393), velocity 0, colour 0.  The colours come from the reference's
-// image input (initParticlesfromPic), which is not built; without an image
-// the reference's colours are zero too (KaminoParticles.cu:73-78).
+// 373-393), velocity 0, and the colour the reference writes: components
+// colorBGR[3i+1], [3i+2], [3i+3] (KaminoSolver.cu:375-377) of its (G, R, B)
+// per-particle array, i.e. (R_i, B_i, G_i+1); for the last particle the third
+// read is past the array in the reference and 0 here.  Without a colour image
+// every colour is 0 (KaminoParticles.cu:73-78); col is then null.
 __global__ void __launch_bounds__(FRAME_THREADS) k_frame_particles(float R, const float2* __restrict__ part,
-                                                                   int64_t n, uint2* __restrict__ out)
+                                                                   const float* __restrict__ col, int64_t n,
+                                                                   uint2* __restrict__ out)
 {
     const int64_t t = (int64_t)blockIdx.x * FRAME_THREADS + threadIdx.x;
     if (t >= n) return;
@@ -121,12 +126,83 @@ __global__ void __launch_bounds__(FRAME_THREADS) k_frame_particles(float R, cons
     sincosf(pt.x, &sp, &cp);
     const float rs = __fmul_rn(R, st);
     const float x = __fmul_rn(rs, cp), z = __fmul_rn(rs, sp), y = __fmul_rn(R, ct);
+    float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
+    if (col) {
+        c0 = __ldg(col + 3 * t + 1);
+        c1 = __ldg(col + 3 * t + 2);
+        c2 = t + 1 < n ? __ldg(col + 3 * t + 3) : 0.0f;
+    }
     uint2* o = out + 5 * t;
     o[0] = make_uint2(be32(x), be32(y));
     o[1] = make_uint2(be32(z), be32(1.0f));
     o[2] = make_uint2(0u, 0u);
-    o[3] = make_uint2(0u, 0u);
-    o[4] = make_uint2(0u, 0u);
+    o[3] = make_uint2(0u, be32(c0));
+    o[4] = make_uint2(be32(c1), be32(c2));
+}
+
+// ------------------------------------------------------------ image input
+// The image of initDensityfromPic / KaminoParticles (KaminoSolver.cu:243-277,
+// KaminoParticles.cu:6-17), decoded by the caller: 8-bit B, G, R pixels.  The
+// reference mirrors it left-right (cv::flip code 1) and resamples it to
+// nPhi x nTheta (cv::resize, INTER_LINEAR).  Here the resampling is bilinear
+// at half-pixel centres with the edges clamped, separable in the order
+// columns then rows, in FP32 with each product and sum rounded as written,
+// and each channel rounded to the nearest 8-bit value (ties to even).  The
+// per-column and per-row source indices (already mirrored) and weights come
+// from the host (image_axis).
+struct ImgAxis {
+    int i0, i1;  // source pixels
+    float a;     // weight of i1
+};
+
+__device__ __forceinline__ float lerp_px(float p0, float p1, float a)
+{
+    return __fadd_rn(__fmul_rn(p0, __fsub_rn(1.0f, a)), __fmul_rn(p1, a));
+}
+
+// One thread per destination pixel (i, j); writes the pixel (B, G, R, 0) to
+// px and, with rho, the thickness (B + G + R) / 3 of KaminoSolver.cu:265-273:
+// each channel / 255.0 rounded to float, a float sum, / 3.0 in double.
+__global__ void __launch_bounds__(FRAME_THREADS) k_image_resample(KGeo g, const uint8_t* __restrict__ img,
+                                                                  size_t stride, const ImgAxis* __restrict__ ax,
+                                                                  const ImgAxis* __restrict__ ay,
+                                                                  uchar4* __restrict__ px, float* __restrict__ rho)
+{
+    const int t = blockIdx.x * FRAME_THREADS + threadIdx.x;
+    if (t >= g.nt * g.np) return;
+    const int j = t >> (g.log2nt + 1), i = t & g.mask;
+    const ImgAxis x = ax[i], y = ay[j];
+    const uint8_t* r0 = img + (size_t)y.i0 * stride;
+    const uint8_t* r1 = img + (size_t)y.i1 * stride;
+    uint8_t c[3];
+    for (int k = 0; k < 3; k++) {
+        const float h0 = lerp_px(r0[3 * x.i0 + k], r0[3 * x.i1 + k], x.a);
+        const float h1 = lerp_px(r1[3 * x.i0 + k], r1[3 * x.i1 + k], x.a);
+        c[k] = (uint8_t)min(255, max(0, __float2int_rn(lerp_px(h0, h1, y.a))));
+    }
+    px[t] = make_uchar4(c[0], c[1], c[2], 0);
+    if (rho) {
+        const float B = (float)__ddiv_rn((double)c[0], 255.0), G = (float)__ddiv_rn((double)c[1], 255.0),
+                    R = (float)__ddiv_rn((double)c[2], 255.0);
+        rho[(size_t)j * g.pitch + i] = (float)__ddiv_rn((double)__fadd_rn(__fadd_rn(B, G), R), 3.0);
+    }
+}
+
+// KaminoParticles.cu:56-57, 64-72: a particle's pixel is its cell
+// floor(phi / gridLen), floor(theta / gridLen) (clamped to the grid; the
+// reference would read outside the image there), colour (G, R, B) / 255.
+__global__ void __launch_bounds__(FRAME_THREADS) k_particle_colors(KGeo g, const float2* __restrict__ part, int64_t n,
+                                                                   const uchar4* __restrict__ px, float* __restrict__ col)
+{
+    const int64_t t = (int64_t)blockIdx.x * FRAME_THREADS + threadIdx.x;
+    if (t >= n) return;
+    const float2 pt = __ldg(part + t);
+    const int xi = min(g.np - 1, max(0, (int)floorf(__fdiv_rn(pt.x, g.h))));
+    const int yi = min(g.nt - 1, max(0, (int)floorf(__fdiv_rn(pt.y, g.h))));
+    const uchar4 p = px[(size_t)yi * g.np + xi];
+    col[3 * t] = (float)__ddiv_rn((double)p.y, 255.0);
+    col[3 * t + 1] = (float)__ddiv_rn((double)p.z, 255.0);
+    col[3 * t + 2] = (float)__ddiv_rn((double)p.x, 255.0);
 }
 
 void put16(std::vector<uint8_t>& o, uint16_t x)
@@ -188,6 +264,7 @@ struct KFrames {
     size_t rec_bytes[2] = {0, 0};
     cudaStream_t copy = nullptr;
     cudaEvent_t packed = nullptr;
+    float* colors = nullptr;  // per-particle (G, R, B) from a colour image, or null
 };
 
 void kamino_frames_release(KFrames* f)
@@ -202,6 +279,7 @@ void kamino_frames_release(KFrames* f)
         }
     if (f->packed) cudaEventDestroy(f->packed);
     if (f->copy) cudaStreamDestroy(f->copy);
+    if (f->colors) cudaFree(f->colors);
     delete f;
 }
 
@@ -272,7 +350,8 @@ int prepare_slot(KFrames* f, const KGeo& g, const KBufs& b, int kind, KFrameSlot
     return KAMINO_OK;
 }
 
-int launch_pack(const KGeo& g, const KBufs& b, int cur_uv, int cur_r, int kind, void* dev, cudaStream_t st)
+int launch_pack(const KGeo& g, const KBufs& b, int cur_uv, int cur_r, int kind, void* dev, cudaStream_t st,
+                const float* colors)
 {
     const int64_t n = frame_points(g, b, kind);
     if (n == 0) return KAMINO_OK;
@@ -280,7 +359,7 @@ int launch_pack(const KGeo& g, const KBufs& b, int cur_uv, int cur_r, int kind, 
     if (kind == KAMINO_FRAME_GRID)
         k_frame_grid<<<blocks, FRAME_THREADS, 0, st>>>(g, b.u[cur_uv], b.v[cur_uv], b.rho[cur_r], (uint4*)dev);
     else
-        k_frame_particles<<<blocks, FRAME_THREADS, 0, st>>>(g.R, b.part[cur_r], n, (uint2*)dev);
+        k_frame_particles<<<blocks, FRAME_THREADS, 0, st>>>(g.R, b.part[cur_r], colors, n, (uint2*)dev);
     FCUDA(cudaGetLastError());
     return KAMINO_OK;
 }
@@ -302,7 +381,7 @@ int capture(kamino_handle h, KFrames* f, int kind)
     cudaStream_t st = kamino_internal_stream(h);
     // The slot's device records were last read by its previous copy, which
     // finished before that capture was written (kamino_frame_write waits).
-    if ((rc = launch_pack(g, b, cu, cr, kind, s.dev, st))) return rc;
+    if ((rc = launch_pack(g, b, cu, cr, kind, s.dev, st, f->colors))) return rc;
     FCUDA(cudaEventRecord(f->packed, st));
     FCUDA(cudaStreamWaitEvent(f->copy, f->packed, 0));
     const size_t rec = f->rec_bytes[kind];
@@ -470,7 +549,7 @@ extern "C" int kamino_frame_time_pack(kamino_handle h, int kind, int reps, int f
     for (int r = 0; r < reps && !rc; r++) {
         if (flush_l2 && (rc = kamino_internal_flush_l2(h))) break;
         cudaEventRecord(e0, st);
-        rc = launch_pack(g, b, cu, cr, kind, s.dev, st);
+        rc = launch_pack(g, b, cu, cr, kind, s.dev, st, f->colors);
         cudaEventRecord(e1, st);
         float t = 0.0f;
         if (!rc && cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&t, e0, e1) == cudaSuccess)
@@ -483,4 +562,134 @@ extern "C" int kamino_frame_time_pack(kamino_handle h, int kind, int reps, int f
     if (rc) return rc;
     *ms = total / reps;
     return KAMINO_OK;
+}
+
+// ------------------------------------------------------------ image input
+namespace {
+
+// Source pixels and weight of each destination column (or row), as
+// cv::resize INTER_LINEAR places them: f = (d + 0.5) * (src / dst) - 0.5 in
+// double, rounded to float; s = floor(f), a = f - s; clamped at both edges
+// with a = 0.  mirror counts the columns from the right (cv::flip code 1).
+std::vector<ImgAxis> image_axis(int src, int dst, bool mirror)
+{
+    std::vector<ImgAxis> ax((size_t)dst);
+    const double scale = (double)src / dst;
+    for (int d = 0; d < dst; d++) {
+        const float f = (float)((d + 0.5) * scale - 0.5);
+        int s0 = (int)std::floor(f);
+        float a = f - (float)s0;
+        if (s0 < 0) {
+            s0 = 0;
+            a = 0.0f;
+        }
+        if (s0 >= src - 1) {
+            s0 = src - 1;
+            a = 0.0f;
+        }
+        int s1 = std::min(s0 + 1, src - 1);
+        if (mirror) {
+            s0 = src - 1 - s0;
+            s1 = src - 1 - s1;
+        }
+        ax[(size_t)d] = {s0, s1, a};
+    }
+    return ax;
+}
+
+// Uploads the image and the axis tables into one scratch allocation and runs
+// k_image_resample; on success *scratch holds the allocation, *px the
+// nPhi x nTheta resampled pixels inside it (the caller frees *scratch).
+int resample(kamino_handle h, const uint8_t* bgr, int width, int height, size_t stride, float* rho, void** scratch,
+             uchar4** px)
+{
+    *scratch = nullptr;
+    if (!bgr || width < 1 || height < 1 || (int64_t)width * height > ((int64_t)1 << 28) ||
+        stride < 3 * (size_t)width)
+        return kamino_fail(KAMINO_ERR_INVALID, "image %dx%d with row stride %zu: bad size or null pixels", width,
+                           height, stride);
+    KGeo g;
+    int rc = kamino_internal_desc(h, &g, nullptr, nullptr, nullptr, nullptr);
+    if (rc) return rc;
+    const std::vector<ImgAxis> ax = image_axis(width, g.np, true), ay = image_axis(height, g.nt, false);
+    auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t row = 3 * (size_t)width, img_b = up(row * height), ax_b = up(sizeof(ImgAxis) * ax.size()),
+                 ay_b = up(sizeof(ImgAxis) * ay.size()), px_b = sizeof(uchar4) * (size_t)g.np * g.nt;
+    char* d = nullptr;
+    cudaError_t e = cudaMalloc((void**)&d, img_b + ax_b + ay_b + px_b);
+    if (e != cudaSuccess) return kamino_fail(KAMINO_ERR_ALLOC, "image scratch: %s", cudaGetErrorString(e));
+    *scratch = d;
+    cudaStream_t st = kamino_internal_stream(h);
+    FCUDA(cudaMemcpy2DAsync(d, row, bgr, stride, row, height, cudaMemcpyHostToDevice, st));
+    FCUDA(cudaMemcpyAsync(d + img_b, ax.data(), sizeof(ImgAxis) * ax.size(), cudaMemcpyHostToDevice, st));
+    FCUDA(cudaMemcpyAsync(d + img_b + ax_b, ay.data(), sizeof(ImgAxis) * ay.size(), cudaMemcpyHostToDevice, st));
+    *px = (uchar4*)(d + img_b + ax_b + ay_b);
+    const unsigned blocks = (unsigned)(((size_t)g.np * g.nt + FRAME_THREADS - 1) / FRAME_THREADS);
+    k_image_resample<<<blocks, FRAME_THREADS, 0, st>>>(g, (const uint8_t*)d, row, (const ImgAxis*)(d + img_b),
+                                                       (const ImgAxis*)(d + img_b + ax_b), *px, rho);
+    FCUDA(cudaGetLastError());
+    return KAMINO_OK;
+}
+
+int finish_image(kamino_handle h, int rc, void* scratch)
+{
+    if (!rc) {
+        const cudaError_t e = cudaStreamSynchronize(kamino_internal_stream(h));
+        if (e != cudaSuccess) rc = kamino_fail(KAMINO_ERR_CUDA, "image input: %s", cudaGetErrorString(e));
+    } else {
+        cudaStreamSynchronize(kamino_internal_stream(h));
+    }
+    if (scratch) cudaFree(scratch);
+    return rc;
+}
+
+}  // namespace
+
+// KaminoSolver::initDensityfromPic (KaminoSolver.cu:243-277) with a decoded
+// image: the thickness of every cell from the mirrored, resampled image.
+extern "C" int kamino_init_density_image(kamino_handle h, const uint8_t* bgr, int width, int height, size_t stride)
+{
+    KFrames* f;
+    int rc = frame_state(h, &f);  // makes the handle's device current
+    if (rc) return rc;
+    KBufs b;
+    int cr;
+    if ((rc = kamino_internal_desc(h, nullptr, &b, nullptr, nullptr, &cr))) return rc;
+    void* scratch = nullptr;
+    uchar4* px = nullptr;
+    rc = resample(h, bgr, width, height, stride, b.rho[cr], &scratch, &px);
+    return finish_image(h, rc, scratch);
+}
+
+// The colours KaminoParticles takes from its image (KaminoParticles.cu:6-17,
+// 56-72) for the particles as they are now.
+extern "C" int kamino_init_particle_colors_image(kamino_handle h, const uint8_t* bgr, int width, int height,
+                                                 size_t stride)
+{
+    KFrames* f;
+    int rc = frame_state(h, &f);
+    if (rc) return rc;
+    KGeo g;
+    KBufs b;
+    int cr;
+    if ((rc = kamino_internal_desc(h, &g, &b, nullptr, nullptr, &cr))) return rc;
+    if (b.npart == 0) return KAMINO_OK;
+    if (!f->colors) {
+        const cudaError_t e = cudaMalloc((void**)&f->colors, sizeof(float) * 3 * (size_t)b.npart);
+        if (e != cudaSuccess) {
+            f->colors = nullptr;
+            return kamino_fail(KAMINO_ERR_ALLOC, "particle colours: %s", cudaGetErrorString(e));
+        }
+    }
+    void* scratch = nullptr;
+    uchar4* px = nullptr;
+    rc = resample(h, bgr, width, height, stride, nullptr, &scratch, &px);
+    if (!rc) {
+        const unsigned blocks = (unsigned)((b.npart + FRAME_THREADS - 1) / FRAME_THREADS);
+        k_particle_colors<<<blocks, FRAME_THREADS, 0, kamino_internal_stream(h)>>>(g, b.part[cr], b.npart, px,
+                                                                                   f->colors);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = kamino_fail(KAMINO_ERR_CUDA, "particle colours: %s", cudaGetErrorString(e));
+    }
+    return finish_image(h, rc, scratch);
 }

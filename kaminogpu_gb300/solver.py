@@ -147,12 +147,21 @@ class KaminoSolver:
         """The reference's FBM curl-noise velocity (kamino_init_fbm)."""
         check(lib.kamino_init_fbm(self._h))
 
-    def initParticlesfromPic(self, path="", seed=1):
-        """KaminoSolver::initParticlesfromPic without an image: the reference's
-        jittered particle placement (kamino_init_particles)."""
-        if path:
-            raise ValueError("image input is not supported")
+    def initParticlesfromPic(self, image=None, seed=1):
+        """KaminoSolver::initParticlesfromPic: the reference's jittered
+        particle placement (kamino_init_particles) and, given a decoded image
+        (uint8 [height, width, 3], B G R), the particles' colours from it."""
         check(lib.kamino_init_particles(self._h, seed))
+        if image is not None:
+            a = np.ascontiguousarray(image, np.uint8)
+            check(lib.kamino_init_particle_colors_image(self._h, a.ctypes.data, a.shape[1], a.shape[0], a.strides[0]))
+
+    def initDensityfromPic(self, image):
+        """KaminoSolver::initDensityfromPic with a decoded image (uint8
+        [height, width, 3], B G R): the thickness from the mirrored, resampled
+        image (kamino_init_density_image)."""
+        a = np.ascontiguousarray(image, np.uint8)
+        check(lib.kamino_init_density_image(self._h, a.ctypes.data, a.shape[1], a.shape[0], a.strides[0]))
 
     def step_host(self, u_phi, u_theta, thickness, dt=None):
         """One step with the state in host memory (kamino_step_host): uploads

@@ -931,3 +931,66 @@ int64_t oracle_ref_particles(float particleDensity, int nTheta, unsigned seed, f
     }
     return (int64_t)numThetaParticles * numPhiParticles;
 }
+
+/* Image input (KaminoSolver::initDensityfromPic, KaminoSolver.cu:243-277;
+ * KaminoParticles' colours, KaminoParticles.cu:6-17, 56-72), restated for
+ * the library's resampling: the image mirrored left-right (cv::flip code 1)
+ * and resampled to dw x dh pixels bilinearly at half-pixel centres with the
+ * edges clamped (cv::resize INTER_LINEAR placement), columns then rows, in
+ * float with -ffp-contract=off, each channel rounded to nearest (ties to
+ * even) and clamped to 8 bits.  OpenCV's own 8-bit path uses fixed-point
+ * weights, so its pixels can differ from these by one level.
+ * out: dw * dh pixels of 3 bytes (B, G, R), rows of dw. */
+static void o_axis(int src, int dst, int mirror, int *i0, int *i1, float *a)
+{
+    const double scale = (double)src / dst;
+    for (int d = 0; d < dst; d++) {
+        const float f = (float)((d + 0.5) * scale - 0.5);
+        int s0 = (int)floorf(f);
+        float w = f - (float)s0;
+        if (s0 < 0) {
+            s0 = 0;
+            w = 0.0f;
+        }
+        if (s0 >= src - 1) {
+            s0 = src - 1;
+            w = 0.0f;
+        }
+        int s1 = s0 + 1 < src - 1 ? s0 + 1 : src - 1;
+        if (mirror) {
+            s0 = src - 1 - s0;
+            s1 = src - 1 - s1;
+        }
+        i0[d] = s0;
+        i1[d] = s1;
+        a[d] = w;
+    }
+}
+
+void oracle_image_resample(const unsigned char *img, int w, int h, size_t stride, int dw, int dh,
+                           unsigned char *out)
+{
+    int *xi0 = malloc(sizeof(int) * dw), *xi1 = malloc(sizeof(int) * dw);
+    int *yi0 = malloc(sizeof(int) * dh), *yi1 = malloc(sizeof(int) * dh);
+    float *xa = malloc(sizeof(float) * dw), *ya = malloc(sizeof(float) * dh);
+    o_axis(w, dw, 1, xi0, xi1, xa);
+    o_axis(h, dh, 0, yi0, yi1, ya);
+    for (int j = 0; j < dh; j++) {
+        const unsigned char *r0 = img + (size_t)yi0[j] * stride, *r1 = img + (size_t)yi1[j] * stride;
+        for (int i = 0; i < dw; i++) {
+            for (int k = 0; k < 3; k++) {
+                const float ax = xa[i], ay = ya[j];
+                const float h0 = (float)r0[3 * xi0[i] + k] * (1.0f - ax) + (float)r0[3 * xi1[i] + k] * ax;
+                const float h1 = (float)r1[3 * xi0[i] + k] * (1.0f - ax) + (float)r1[3 * xi1[i] + k] * ax;
+                long v = lrintf(h0 * (1.0f - ay) + h1 * ay);
+                out[3 * ((size_t)j * dw + i) + k] = (unsigned char)(v < 0 ? 0 : v > 255 ? 255 : v);
+            }
+        }
+    }
+    free(xi0);
+    free(xi1);
+    free(yi0);
+    free(yi1);
+    free(xa);
+    free(ya);
+}

@@ -57,6 +57,7 @@ def _oracle_lib():
         L.oracle_frame_particles.argtypes = [_F, _P, _I64, _P]
         L.oracle_ref_particles.argtypes = [_F, _I, ctypes.c_uint, _P]
         L.oracle_ref_particles.restype = _I64
+        L.oracle_image_resample.argtypes = [_P, _I, _I, ctypes.c_size_t, _I, _I, _P]
         _olib = L
     return _olib
 
@@ -202,6 +203,44 @@ def ref_particles(particle_density, nt, seed=1):
     n = L.oracle_ref_particles(float(d), nt, seed, out.ctypes.data)
     assert n == out.shape[0]
     return out
+
+
+def image_resample(img, dw, dh):
+    """The mirrored, resampled 8-bit image (oracle_image_resample): uint8
+    [dh, dw, 3] from uint8 [h, w, 3] (B, G, R)."""
+    L = _oracle_lib()
+    img = np.ascontiguousarray(img, np.uint8)
+    out = np.empty((dh, dw, 3), np.uint8)
+    L.oracle_image_resample(img.ctypes.data, img.shape[1], img.shape[0], img.strides[0], dw, dh, out.ctypes.data)
+    return out
+
+
+def image_density(px):
+    """initDensityfromPic's per-cell value (KaminoSolver.cu:265-273): each
+    channel / 255.0 rounded to float, a float sum, / 3.0 rounded to float."""
+    c = (px.astype(np.float64) / 255.0).astype(np.float32)
+    s = (c[..., 0] + c[..., 1]) + c[..., 2]
+    return (s.astype(np.float64) / 3.0).astype(np.float32)
+
+
+def particle_colors(px, part, nt):
+    """KaminoParticles' colours (KaminoParticles.cu:56-72): (G, R, B) / 255
+    of the pixel of each particle's cell, float32 [n, 3]."""
+    h = grid_h(nt)
+    part = np.asarray(part, np.float32).reshape(-1, 2)
+    x = np.clip(np.floor(part[:, 0] / h).astype(np.int64), 0, 2 * nt - 1)
+    y = np.clip(np.floor(part[:, 1] / h).astype(np.int64), 0, nt - 1)
+    p = px[y, x].astype(np.float64) / 255.0
+    return np.stack([p[:, 1], p[:, 2], p[:, 0]], 1).astype(np.float32)
+
+
+def written_colors(col):
+    """The colour write_particles_bgeo writes for particle i: components
+    3i+1, 3i+2, 3i+3 of the flat (G, R, B) array (KaminoSolver.cu:375-377);
+    the last particle's third one lies past the array (0 here)."""
+    flat = np.concatenate([np.asarray(col, np.float32).reshape(-1), np.zeros(1, np.float32)])
+    n = len(col)
+    return np.stack([flat[3 * np.arange(n) + k] for k in (1, 2, 3)], 1)
 
 
 def bgeo_image(records, attrs):

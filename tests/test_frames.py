@@ -125,3 +125,44 @@ def test_cli_usage_and_config_errors(kg, tmp_path):
     bad.write_text("1.0 32 1.0\n")
     r = subprocess.run([exe, str(bad)], capture_output=True, text=True)
     assert r.returncode == 1 and "16 whitespace-separated fields" in r.stderr
+
+
+def numpy_resample(img, dw, dh):
+    """Mirrored bilinear resampling at half-pixel centres, edges clamped,
+    columns then rows, float32 per operation, round half to even."""
+    h, w = img.shape[:2]
+
+    def axis(src, dst, mirror):
+        f = ((np.arange(dst) + 0.5) * (src / dst) - 0.5).astype(np.float32)
+        s0 = np.floor(f).astype(np.int64)
+        a = (f - s0.astype(np.float32)).astype(np.float32)
+        a[s0 < 0] = 0
+        s0[s0 < 0] = 0
+        a[s0 >= src - 1] = 0
+        s0[s0 >= src - 1] = src - 1
+        s1 = np.minimum(s0 + 1, src - 1)
+        return (src - 1 - s0, src - 1 - s1, a) if mirror else (s0, s1, a)
+
+    x0, x1, ax = axis(w, dw, True)
+    y0, y1, ay = axis(h, dh, False)
+    f = img.astype(np.float32)
+    one = np.float32(1)
+    bx, by = ax[None, :, None], ay[:, None, None]
+    h0 = f[y0][:, x0] * (one - bx) + f[y0][:, x1] * bx
+    h1 = f[y1][:, x0] * (one - bx) + f[y1][:, x1] * bx
+    return np.clip(np.rint(h0 * (one - by) + h1 * by), 0, 255).astype(np.uint8)
+
+
+@pytest.mark.parametrize("w,h,dw,dh", [(100, 37, 128, 64), (256, 128, 128, 64), (128, 64, 128, 64),
+                                       (31, 300, 64, 32), (1, 1, 64, 32)])
+def test_oracle_image_resample(orc, w, h, dw, dh):
+    rng = np.random.default_rng(w * h)
+    img = rng.integers(0, 256, (h, w, 3), dtype=np.uint8)
+    got = orc.image_resample(img, dw, dh)
+    assert np.array_equal(got, numpy_resample(img, dw, dh))
+    if (w, h) == (dw, dh):  # same size: the mirrored image itself
+        assert np.array_equal(got, img[:, ::-1])
+    flat = orc.image_resample(np.full((h, w, 3), 77, np.uint8), dw, dh)
+    assert (flat == 77).all()
+    d = orc.image_density(got)
+    assert d.shape == (dh, dw) and d.min() >= 0 and d.max() <= 1

@@ -150,3 +150,68 @@ def test_cli_runs_the_reference_frame_loop(kg, orc, tmp_path):
     want = orc.frame_particle_records(part0, 1.0)
     assert rec.shape[0] == kg.particle_count(cfg) == 2 * 32 * 32
     assert np.abs(rec[:, :3] - want[:, :3]).max() <= POS_ULPS
+
+
+@pytest.mark.parametrize("w,h,nt", [(100, 37, 64), (256, 128, 64), (3000, 1500, 1024)])
+def test_density_image_matches_oracle(kg, orc, w, h, nt):
+    """initDensityfromPic (KaminoSolver.cu:243-277) on the device: the
+    thickness equals the oracle's mirrored, resampled image averaged over the
+    channels, bit for bit."""
+    rng = np.random.default_rng(w + h)
+    img = rng.integers(0, 256, (h, w, 3), dtype=np.uint8)
+    cfg = kg.default_config(n_theta=nt, radius=1.0, dt=0.005, n_particles=0)
+    with kg.KaminoSolver(config=cfg) as s:
+        s.initDensityfromPic(img)
+        got = s.get_state(kg.THICKNESS)
+    want = orc.image_density(orc.image_resample(img, 2 * nt, nt))
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_particle_colors_reach_the_particle_frames(kg, orc):
+    nt = 32
+    rng = np.random.default_rng(9)
+    img = rng.integers(0, 256, (45, 70, 3), dtype=np.uint8)
+    cfg = kg.default_config(n_theta=nt, radius=1.0, dt=0.005, particle_density=2.0, n_particles=-1)
+    with kg.KaminoSolver(config=cfg) as s:
+        s.initParticlesfromPic(img)
+        part = s.get_state(kg.PARTICLES)
+        _, rec = orc.read_bgeo(s.write_frame(kg.FRAME_PARTICLES))
+    col = orc.particle_colors(orc.image_resample(img, 2 * nt, nt), part, nt)
+    want = orc.written_colors(col)
+    assert np.array_equal(rec[:, 7:10].view(np.uint32), want.view(np.uint32))
+    assert rec[:-1, 7:10].any(axis=1).mean() > 0.9 and rec[-1, 9] == 0
+
+
+def write_ppm(path, bgr):
+    h, w = bgr.shape[:2]
+    path.write_bytes(b"P6\n# test image\n%d %d\n255\n" % (w, h) + np.ascontiguousarray(bgr[..., ::-1]).tobytes())
+
+
+def test_cli_reads_ppm_images(kg, orc, tmp_path):
+    import subprocess
+    nt, frames = 32, 2
+    rng = np.random.default_rng(12)
+    dimg = rng.integers(0, 256, (50, 90, 3), dtype=np.uint8)
+    cimg = rng.integers(0, 256, (20, 33, 3), dtype=np.uint8)
+    write_ppm(tmp_path / "d.ppm", dimg)
+    write_ppm(tmp_path / "c.ppm", cimg)
+    cfgfile = tmp_path / "configKamino.txt"
+    cfgfile.write_text("1.0 %d 1.0 0.005 0.01 %d 0.0 1 1 1 1 %s %s %s null %s\n"
+                       % (nt, frames, tmp_path / "g_", tmp_path / "p_", tmp_path / "d.ppm", tmp_path / "c.ppm"))
+    exe = os.path.join(os.path.dirname(kg.LIB_PATH), "kamino")
+    r = subprocess.run([exe, str(cfgfile)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert "ignored" not in r.stderr
+    cfg = kg.parse_config(cfgfile)
+    with kg.KaminoSolver(config=cfg) as s:
+        s.init_fbm()
+        s.initDensityfromPic(dimg)
+        s.initParticlesfromPic(cimg)
+        rho0 = s.get_state(kg.THICKNESS)
+        s.run_frames_bgeo(frames, str(tmp_path / "lg_"), str(tmp_path / "lp_"))
+    for i in range(frames + 1):
+        assert (tmp_path / ("g_%d.bgeo" % i)).read_bytes() == (tmp_path / ("lg_%d.bgeo" % i)).read_bytes(), i
+        assert (tmp_path / ("p_%d.bgeo" % i)).read_bytes() == (tmp_path / ("lp_%d.bgeo" % i)).read_bytes(), i
+    _, rec = orc.read_bgeo((tmp_path / "g_0.bgeo").read_bytes())
+    assert np.array_equal(rec[:, 7], rho0.reshape(-1))
+    assert np.array_equal(rho0, orc.image_density(orc.image_resample(dimg, 2 * nt, nt)))
