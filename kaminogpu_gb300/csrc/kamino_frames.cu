@@ -497,29 +497,45 @@ extern "C" int kamino_run_frames_bgeo(kamino_handle h, int frames, const char* g
         if (want[k] && f->slot[k][f->tail[k]].pending)
             return kamino_fail(KAMINO_ERR_INVALID, "a captured frame of kind %d is not yet written", k);
     auto name = [&](int k, int i) { return std::string(base[k]) + std::to_string(i) + ".bgeo"; };
-    for (int k = 0; k < 2; k++)
-        if (want[k] && (rc = capture(h, f, k))) return rc;
-    const float fdt = (float)dt, fDT = (float)DT;
-    float T = 0.0f;
     int64_t total = 0;
-    for (int i = 1; i <= frames; i++) {
-        int64_t n = 0;  // the reference's step count for frame i (KaminoCore.cu:888-895)
-        while (T < i * fDT) {
-            n++;
-            T += fdt;
-        }
-        n++;
-        T = i * fDT;
-        if (n > 0x7fffffff) return kamino_fail(KAMINO_ERR_INVALID, "too many steps in a frame");
-        if ((rc = kamino_step_n(h, (int)n))) return rc;
-        total += n;
+    auto run = [&]() {
+        int r;
         for (int k = 0; k < 2; k++)
-            if (want[k] && (rc = capture(h, f, k))) return rc;
-        for (int k = 0; k < 2; k++)  // frame i-1, while frame i runs
-            if (want[k] && (rc = finish(h, f, k, name(k, i - 1).c_str(), nullptr, 0))) return rc;
+            if (want[k] && (r = capture(h, f, k))) return r;
+        const float fdt = (float)dt, fDT = (float)DT;
+        float T = 0.0f;
+        for (int i = 1; i <= frames; i++) {
+            int64_t n = 0;  // the reference's step count for frame i (KaminoCore.cu:888-895)
+            while (T < i * fDT) {
+                n++;
+                T += fdt;
+            }
+            n++;
+            T = i * fDT;
+            if (n > 0x7fffffff) return kamino_fail(KAMINO_ERR_INVALID, "too many steps in a frame");
+            if ((r = kamino_step_n(h, (int)n))) return r;
+            total += n;
+            for (int k = 0; k < 2; k++)
+                if (want[k] && (r = capture(h, f, k))) return r;
+            for (int k = 0; k < 2; k++)  // frame i-1, while frame i runs
+                if (want[k] && (r = finish(h, f, k, name(k, i - 1).c_str(), nullptr, 0))) return r;
+        }
+        for (int k = 0; k < 2; k++)
+            if (want[k] && (r = finish(h, f, k, name(k, frames).c_str(), nullptr, 0))) return r;
+        return (int)KAMINO_OK;
+    };
+    rc = run();
+    if (rc) {  // leave no capture of this loop waiting: later captures and loops start clean
+        for (int k = 0; k < 2; k++) {
+            if (!want[k]) continue;
+            for (auto& sl : f->slot[k]) {
+                if (sl.pending) cudaEventSynchronize(sl.copied);
+                sl.pending = false;
+            }
+            f->head[k] = f->tail[k] = 0;
+        }
+        return rc;
     }
-    for (int k = 0; k < 2; k++)
-        if (want[k] && (rc = finish(h, f, k, name(k, frames).c_str(), nullptr, 0))) return rc;
     if (steps_taken) *steps_taken = total;
     return KAMINO_OK;
 }

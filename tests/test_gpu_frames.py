@@ -109,10 +109,17 @@ def test_run_frames_bgeo_writes_every_frame(kg, orc, tmp_path):
 
 
 def test_frame_write_reports_io_errors(kg, tmp_path):
-    with make_solver(kg, 32) as s:
+    with make_solver(kg, 32, npart=256, frame_dt=0.012) as s:
         with pytest.raises(kg.KaminoError) as e:
             s.write_frame(kg.FRAME_GRID, path=tmp_path / "missing_dir" / "f.bgeo")
         assert e.value.code == kg._lib.ERR_IO and "cannot open" in str(e.value)
+        # a frame loop that fails leaves no capture waiting behind it
+        with pytest.raises(kg.KaminoError) as e:
+            s.run_frames_bgeo(2, str(tmp_path / "missing_dir" / "g_"), str(tmp_path / "p_"))
+        assert e.value.code == kg._lib.ERR_IO
+        s.run_frames_bgeo(1, str(tmp_path / "g_"), str(tmp_path / "p_"))
+        now = s.write_frame(kg.FRAME_GRID)
+    assert (tmp_path / "g_1.bgeo").read_bytes() == now
 
 
 def test_init_particles_uploads_the_reference_placement(kg, orc):
