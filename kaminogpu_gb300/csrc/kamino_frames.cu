@@ -328,25 +328,31 @@ int frame_state(kamino_handle h, KFrames** out)
 // trailer once (they depend only on the point count, fixed per handle).
 int prepare_slot(KFrames* f, const KGeo& g, const KBufs& b, int kind, KFrameSlot& s)
 {
-    if (s.host) return KAMINO_OK;
+    if (s.host) return KAMINO_OK;  // set only once every buffer of the slot exists
     const std::vector<uint8_t> head = frame_header(g, b, kind);
     const size_t rec = (size_t)frame_points(g, b, kind) * record_bytes(kind);
     const size_t pad = (256 - head.size() % 256) % 256;
+    void* dp = nullptr;
+    void* hp = nullptr;
+    cudaEvent_t ev = nullptr;
+    cudaError_t e = rec ? cudaMalloc(&dp, rec) : cudaSuccess;
+    if (e == cudaSuccess) e = cudaHostAlloc(&hp, pad + head.size() + rec + 2, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        if (dp) cudaFree(dp);
+        if (hp) cudaFreeHost(hp);
+        return kamino_fail(KAMINO_ERR_ALLOC, "frame buffers (%zu bytes): %s", rec, cudaGetErrorString(e));
+    }
+    uint8_t* host = (uint8_t*)hp;
+    std::memcpy(host + pad, head.data(), head.size());
+    host[pad + head.size() + rec] = 0x00;
+    host[pad + head.size() + rec + 1] = 0xff;
+    s.dev = dp;
+    s.copied = ev;
     s.file_off = pad;
     s.file_bytes = head.size() + rec + 2;
+    s.host = host;
     f->rec_bytes[kind] = rec;
-    void* hp = nullptr;
-    FCUDA(cudaHostAlloc(&hp, pad + s.file_bytes, cudaHostAllocDefault));
-    s.host = (uint8_t*)hp;
-    if (rec) {
-        cudaError_t e = cudaMalloc(&s.dev, rec);
-        if (e != cudaSuccess) return kamino_fail(KAMINO_ERR_ALLOC, "frame records (%zu bytes): %s", rec,
-                                                 cudaGetErrorString(e));
-    }
-    FCUDA(cudaEventCreateWithFlags(&s.copied, cudaEventDisableTiming));
-    std::memcpy(s.host + pad, head.data(), head.size());
-    s.host[pad + head.size() + rec] = 0x00;
-    s.host[pad + head.size() + rec + 1] = 0xff;
     return KAMINO_OK;
 }
 
