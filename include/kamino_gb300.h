@@ -284,6 +284,15 @@ int kamino_run_frames_bgeo(kamino_handle h, int frames, const char* grid_path, c
  * launch, outside the timed interval). */
 int kamino_frame_time_pack(kamino_handle h, int kind, int reps, int flush_l2, double* ms);
 
+/* Checkpoint and resume: no counterpart in the reference (its .bgeo frames
+ * are write-only).  kamino_save_state writes u_phi, u_theta, the thickness,
+ * the particles, the step count and the elapsed time to a file with a
+ * checksum; kamino_load_state restores them into a handle of the same
+ * n_theta, particle count, radius and dt (KAMINO_ERR_INVALID otherwise;
+ * KAMINO_ERR_IO for a truncated or corrupted file).  Synchronous. */
+int kamino_save_state(kamino_handle h, const char* path);
+int kamino_load_state(kamino_handle h, const char* path);
+
 int kamino_synchronize(kamino_handle h);
 
 /* Elapsed simulated time (KaminoSolver.cu:220) and step count. */

@@ -135,6 +135,8 @@ SIGNATURES = {
     "kamino_run_frames_bgeo": (_I, [_P, _I, ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_I64)]),
     "kamino_frame_time_pack": (_I, [_P, _I, _I, _I, ctypes.POINTER(_D)]),
     "kamino_synchronize": (_I, [_P]),
+    "kamino_save_state": (_I, [_P, ctypes.c_char_p]),
+    "kamino_load_state": (_I, [_P, ctypes.c_char_p]),
     "kamino_time_elapsed": (_I, [_P, ctypes.POINTER(_D), ctypes.POINTER(_I64)]),
     "kamino_time_steps": (_I, [_P, _I, _I, ctypes.POINTER(_D)]),
     "kamino_time_kernels": (_I, [_P, _I, _I, ctypes.POINTER(_D), _I, ctypes.POINTER(_I)]),

@@ -430,3 +430,107 @@ extern "C" int kamino_init_particles(kamino_handle h, uint32_t seed)
     if ((rc = kamino_reference_particles(&cfg, seed, buf.data(), n))) return rc;
     return kamino_set_state(h, KAMINO_PARTICLES, buf.data(), 0);
 }
+
+// ------------------------------------------------------- checkpoint / resume
+// A raw dump of one sphere's state, for resuming a run; the reference has no
+// counterpart (its .bgeo frames are write-only).  Layout, native little-endian:
+//   char[8] "KAMINOS1", int32 n_theta, int32 flags, int64 n_particles,
+//   double radius, double dt, int64 steps, double time,
+//   float u_phi[nt][2nt], u_theta[nt-1][2nt], thickness[nt][2nt],
+//   float particles[n][2], uint64 FNV-1a hash of every byte before it.
+namespace {
+
+struct StateHeader {
+    char magic[8];
+    int32_t n_theta;
+    uint32_t flags;
+    int64_t n_particles;
+    double radius, dt;
+    int64_t steps;
+    double time;
+};
+static_assert(sizeof(StateHeader) == 56, "state header layout");
+
+constexpr char kStateMagic[8] = {'K', 'A', 'M', 'I', 'N', 'O', 'S', '1'};
+
+uint64_t fnv1a(const void* p, size_t n, uint64_t hsh)
+{
+    const unsigned char* c = (const unsigned char*)p;
+    for (size_t k = 0; k < n; k++) hsh = (hsh ^ c[k]) * 0x100000001b3ull;
+    return hsh;
+}
+
+constexpr uint64_t kFnvBasis = 0xcbf29ce484222325ull;
+
+}  // namespace
+
+extern "C" int kamino_save_state(kamino_handle h, const char* path)
+{
+    kamino_config cfg;
+    int rc = kamino_internal_config(h, &cfg);
+    if (rc) return rc;
+    if (!path) return kamino_fail(KAMINO_ERR_INVALID, "kamino_save_state: null path");
+    StateHeader hd;
+    std::memcpy(hd.magic, kStateMagic, 8);
+    hd.n_theta = cfg.n_theta;
+    hd.flags = cfg.flags;
+    hd.n_particles = kamino_particle_count(&cfg);
+    hd.radius = cfg.radius;
+    hd.dt = cfg.dt;
+    int cu, cr;
+    if ((rc = kamino_internal_get_counters(h, &cu, &cr, &hd.steps, &hd.time))) return rc;
+    const size_t np = 2 * (size_t)cfg.n_theta, nt = (size_t)cfg.n_theta;
+    std::vector<float> data(np * nt + np * (nt - 1) + np * nt + 2 * (size_t)hd.n_particles);
+    float* p = data.data();
+    if ((rc = kamino_get_state(h, KAMINO_U_PHI, p, 0)) || (rc = kamino_get_state(h, KAMINO_U_THETA, p + np * nt, 0)) ||
+        (rc = kamino_get_state(h, KAMINO_THICKNESS, p + np * (2 * nt - 1), 0)))
+        return rc;
+    if (hd.n_particles && (rc = kamino_get_state(h, KAMINO_PARTICLES, p + np * (3 * nt - 1), 0))) return rc;
+    const uint64_t sum = fnv1a(data.data(), sizeof(float) * data.size(), fnv1a(&hd, sizeof(hd), kFnvBasis));
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) return kamino_fail(KAMINO_ERR_IO, "cannot open %s for writing", path);
+    bool ok = std::fwrite(&hd, sizeof(hd), 1, fp) == 1 &&
+              std::fwrite(data.data(), sizeof(float), data.size(), fp) == data.size() &&
+              std::fwrite(&sum, sizeof(sum), 1, fp) == 1;
+    ok = (std::fclose(fp) == 0) && ok;
+    if (!ok) return kamino_fail(KAMINO_ERR_IO, "short write to %s", path);
+    return KAMINO_OK;
+}
+
+extern "C" int kamino_load_state(kamino_handle h, const char* path)
+{
+    kamino_config cfg;
+    int rc = kamino_internal_config(h, &cfg);
+    if (rc) return rc;
+    if (!path) return kamino_fail(KAMINO_ERR_INVALID, "kamino_load_state: null path");
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) return kamino_fail(KAMINO_ERR_IO, "cannot open %s", path);
+    StateHeader hd;
+    const size_t np = 2 * (size_t)cfg.n_theta, nt = (size_t)cfg.n_theta;
+    const int64_t npart = kamino_particle_count(&cfg);
+    std::vector<float> data(np * nt + np * (nt - 1) + np * nt + 2 * (size_t)npart);
+    uint64_t sum = 0;
+    bool ok = std::fread(&hd, sizeof(hd), 1, fp) == 1 && std::memcmp(hd.magic, kStateMagic, 8) == 0;
+    if (ok && (hd.n_theta != cfg.n_theta || hd.n_particles != npart)) {
+        std::fclose(fp);
+        return kamino_fail(KAMINO_ERR_INVALID, "%s holds nTheta %d with %lld particles; the handle has %d and %lld",
+                           path, hd.n_theta, (long long)hd.n_particles, cfg.n_theta, (long long)npart);
+    }
+    ok = ok && std::fread(data.data(), sizeof(float), data.size(), fp) == data.size() &&
+         std::fread(&sum, sizeof(sum), 1, fp) == 1 && std::fgetc(fp) == EOF;
+    std::fclose(fp);
+    if (!ok) return kamino_fail(KAMINO_ERR_IO, "%s is not a complete state file", path);
+    if (sum != fnv1a(data.data(), sizeof(float) * data.size(), fnv1a(&hd, sizeof(hd), kFnvBasis)))
+        return kamino_fail(KAMINO_ERR_IO, "%s: checksum mismatch", path);
+    if (hd.radius != cfg.radius || hd.dt != cfg.dt)
+        return kamino_fail(KAMINO_ERR_INVALID, "%s: radius %g, dt %g; the handle has radius %g, dt %g", path,
+                           hd.radius, hd.dt, cfg.radius, cfg.dt);
+    const float* p = data.data();
+    if ((rc = kamino_set_state(h, KAMINO_U_PHI, p, 0)) || (rc = kamino_set_state(h, KAMINO_U_THETA, p + np * nt, 0)) ||
+        (rc = kamino_set_state(h, KAMINO_THICKNESS, p + np * (2 * nt - 1), 0)))
+        return rc;
+    if (npart && (rc = kamino_set_state(h, KAMINO_PARTICLES, p + np * (3 * nt - 1), 0))) return rc;
+    int cu, cr;
+    if ((rc = kamino_internal_get_counters(h, &cu, &cr, nullptr, nullptr))) return rc;
+    return kamino_internal_set_counters(h, cu, cr, hd.steps, hd.time);
+}

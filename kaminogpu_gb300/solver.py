@@ -195,6 +195,14 @@ class KaminoSolver:
     def synchronize(self):
         check(lib.kamino_synchronize(self._h))
 
+    def save_state(self, path):
+        """Checkpoint the sphere to a file (kamino_save_state)."""
+        check(lib.kamino_save_state(self._h, str(path).encode()))
+
+    def load_state(self, path):
+        """Resume from a checkpoint of the same configuration (kamino_load_state)."""
+        check(lib.kamino_load_state(self._h, str(path).encode()))
+
     # ------------------------------------------------------- frame output
     def frame_bytes(self, kind=FRAME_GRID):
         n = ctypes.c_size_t()

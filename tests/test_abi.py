@@ -54,5 +54,7 @@ def test_null_handles_are_errors_not_crashes(kg):
     assert kg.lib.kamino_step(None, 0.01) == kg.ERR_INVALID
     assert kg.lib.kamino_set_state(None, 0, None, 0) == kg.ERR_INVALID
     assert kg.lib.kamino_destroy(None) == 0
+    assert kg.lib.kamino_save_state(None, b"x") == kg.ERR_INVALID
+    assert kg.lib.kamino_load_state(None, b"x") == kg.ERR_INVALID
     rc = kg.lib.kamino_projection_noalloc(512, None, None, None, None, None, None)
     assert rc == kg.ERR_INVALID and "n_theta" in kg._lib.last_error()
