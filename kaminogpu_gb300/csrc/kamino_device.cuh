@@ -316,6 +316,9 @@ __device__ __forceinline__ float advect_from(const float* __restrict__ u, const 
 //   centred point:  u = mean of u[j][i..i+1],  v = mean of v[j-1..j][i]
 // The rows next to the poles and the two columns at the phi seam run
 // advect_cell for each quantity.
+// MASK selects the quantities (bit 0 u_phi, bit 1 u_theta, bit 2 thickness);
+// each one's value does not depend on which others are computed.
+template <int MASK = 7>
 __device__ __forceinline__ void advect_cell3(const float* __restrict__ u, const float* __restrict__ v,
                                              const float* __restrict__ rho, int i, int j, float cPc, float cPv,
                                              float cT, const KGeo& g, float& out_u, float& out_v, float& out_r)
@@ -341,14 +344,18 @@ __device__ __forceinline__ void advect_cell3(const float* __restrict__ u, const 
         const unsigned ib = (unsigned)i - (unsigned)kFloorBits, jb = (unsigned)j - (unsigned)kFloorBits;
         const float2 nhc = __fmul2_rn(f2(cPc, cT), f2(-0.5f, -0.5f));
         const float2 nhv = f2(-0.5f * cPv, nhc.y);
-        out_u = advect_from<KIND_VPHI>(u, v, u, i, j, ib, jb, f2(gu_phi, gv_phi), nhc, g, vf);
-        out_v = advect_from<KIND_VTHETA>(u, v, v, i, j, ib, jb, f2(gu_th, gv_th), nhv, g, vf);
-        out_r = advect_from<KIND_CENTERED>(u, v, rho, i, j, ib, jb, f2(gu_c, gv_c), nhc, g, vf);
+        if constexpr ((MASK & 1) != 0)
+            out_u = advect_from<KIND_VPHI>(u, v, u, i, j, ib, jb, f2(gu_phi, gv_phi), nhc, g, vf);
+        if constexpr ((MASK & 2) != 0)
+            out_v = advect_from<KIND_VTHETA>(u, v, v, i, j, ib, jb, f2(gu_th, gv_th), nhv, g, vf);
+        if constexpr ((MASK & 4) != 0)
+            out_r = advect_from<KIND_CENTERED>(u, v, rho, i, j, ib, jb, f2(gu_c, gv_c), nhc, g, vf);
         return;
     }
-    out_u = advect_cell<KIND_VPHI>(u, v, u, i, j, cPc, cT, g);
-    if (j < g.nt - 1) out_v = advect_cell<KIND_VTHETA>(u, v, v, i, j, cPv, cT, g);
-    out_r = advect_cell<KIND_CENTERED>(u, v, rho, i, j, cPc, cT, g);
+    if constexpr ((MASK & 1) != 0) out_u = advect_cell<KIND_VPHI>(u, v, u, i, j, cPc, cT, g);
+    if constexpr ((MASK & 2) != 0)
+        if (j < g.nt - 1) out_v = advect_cell<KIND_VTHETA>(u, v, v, i, j, cPv, cT, g);
+    if constexpr ((MASK & 4) != 0) out_r = advect_cell<KIND_CENTERED>(u, v, rho, i, j, cPc, cT, g);
 }
 
 // PTX rcp.approx.ftz.f32: the hardware reciprocal, within about an ulp.

@@ -195,6 +195,42 @@ __global__ void __launch_bounds__(ADV_THREADS, 8) k_advect(KGeo g, KBufs b, int 
     advect_tile<REF>(g, b, suv, duv, sr, dr, nb_u, nb_v, nb_r, blockIdx.x, threadIdx.x);
 }
 
+// The cell-exact advection split in two launches, for the step with the
+// state in host memory: MASK 3 advects u_phi and u_theta (and the particles,
+// which need only the velocity), MASK 4 the thickness, so the first can run
+// while the thickness is still being copied in.  Each value is the one
+// k_advect<false> computes.
+template <int MASK>
+__global__ void __launch_bounds__(ADV_THREADS, 8) k_advect_part(KGeo g, KBufs b, int suv, int duv, int sr, int dr,
+                                                              int nb_u)
+{
+    pdl_wait();
+    const float* __restrict__ u = b.u[suv];
+    const float* __restrict__ v = b.v[suv];
+    int blk = blockIdx.x;
+    const int tid = threadIdx.x;
+    if (blk < nb_u) {
+        const int idx = blk * ADV_THREADS + tid;
+        if (idx >= g.nt * g.np) return;
+        const int j = idx >> (g.log2nt + 1), i = idx & g.mask;
+        float ou = 0.0f, ov = 0.0f, orr = 0.0f;
+        advect_cell3<MASK>(u, v, b.rho[sr], i, j, __ldg(b.cell_c + j), __ldg(b.cell_v + j), g.cellTheta, g, ou, ov,
+                           orr);
+        if constexpr ((MASK & 1) != 0) b.u[duv][idx] = ou;
+        if constexpr ((MASK & 2) != 0)
+            if (j < g.nt - 1) b.v[duv][idx] = ov;
+        if constexpr ((MASK & 4) != 0) b.rho[dr][idx] = orr;
+        return;
+    }
+    if constexpr ((MASK & 1) != 0) {
+        const int64_t k = (int64_t)(blk - nb_u) * ADV_THREADS + tid;
+        if (k >= b.npart) return;
+        float2 out;
+        advect_particle(g, u, v, b.part[sr][k], out);
+        b.part[dr][k] = out;
+    }
+}
+
 // --------------------------------------------------------------- geometric
 // Elementwise stages take four consecutive cells of a row per thread
 // (float4 loads and stores; rows are nPhi >= 64 floats, 16-byte aligned).

@@ -60,6 +60,9 @@ struct kamino_solver_s {
     size_t smem_div = 0, smem_solve = 0, smem_ifft = 0;
     cudaStream_t io_stream = nullptr;  // kamino_step_host: the early thickness download
     cudaEvent_t ev_adv = nullptr;      // kamino_step_host: the advection has written its fields
+    cudaEvent_t ev_uv = nullptr;       // kamino_step_host: u_phi and u_theta are on the device
+    cudaEvent_t ev_rho = nullptr;      // kamino_step_host: the thickness is on the device
+    cudaEvent_t ev_u = nullptr;        // kamino_step_host: u_phi of the step is final
     KFrames* frames = nullptr;         // frame output (kamino_frames.cu), made on first use
 };
 
@@ -147,7 +150,8 @@ extern "C" int kamino_destroy(kamino_handle h)
     destroy_graphs(h);
     kamino_frames_release(h->frames);
     if (h->io_stream) cudaStreamSynchronize(h->io_stream);
-    if (h->ev_adv) cudaEventDestroy(h->ev_adv);
+    for (cudaEvent_t e : {h->ev_adv, h->ev_uv, h->ev_rho, h->ev_u})
+        if (e) cudaEventDestroy(e);
     if (h->io_stream) cudaStreamDestroy(h->io_stream);
     if (h->arena) cudaFree(h->arena);
     if (h->flush) cudaFree(h->flush);
@@ -481,12 +485,20 @@ static int launch_ifft(kamino_solver_s* h, int uv_in, int uv_out)
     return launched("k_vgrad", e);
 }
 
-// The fused step from parity (cu, cr); ev, when given, receives an external
-// event record before the first and after every kernel (kNumKernels + 1).
+// Events of the step with the state in host memory (kamino_step_host): the
+// advection runs as two launches, u_phi and u_theta first and the thickness
+// once rho_ready (its upload) has completed; u_done is recorded when u_phi is
+// final.
+struct HostIo {
+    cudaEvent_t rho_ready, u_done;
+};
+
 // The six launches of one step from buffer parity (cu, cr).  ev: optional
 // per-kernel timing events (graph capture); after_advect: optional event
-// recorded once the advection has written the step's thickness.
-static int enqueue_step(kamino_solver_s* h, int cu, int cr, cudaEvent_t* ev, cudaEvent_t after_advect = nullptr)
+// recorded once the advection has written the step's thickness; io: the
+// split advection of kamino_step_host (cell-exact sampler only).
+static int enqueue_step(kamino_solver_s* h, int cu, int cr, cudaEvent_t* ev, cudaEvent_t after_advect = nullptr,
+                        const HostIo* io = nullptr)
 {
     cudaError_t pending = cudaGetLastError();
     if (pending != cudaSuccess)
@@ -496,7 +508,21 @@ static int enqueue_step(kamino_solver_s* h, int cu, int cr, cudaEvent_t* ev, cud
         if (ev) cudaEventRecordWithFlags(ev[k], h->stream, cudaEventRecordExternal);
     };
     mark(0);
-    if (!rc) rc = launch_advect(h, cu, 1 - cu, cr, 1 - cr);
+    if (!rc && io) {
+        const KGeo& g = h->g;
+        const int T = kk::ADV_THREADS;
+        const int nb_u = (g.nt * g.np + T - 1) / T, nb_p = (int)((h->b.npart + T - 1) / T);
+        cudaError_t e = kk::launch_pdl(kk::k_advect_part<3>, nb_u + nb_p, T, 0, h->stream, g, h->b, cu, 1 - cu, cr,
+                                       1 - cr, nb_u);
+        rc = launched("k_advect_part<3>", e);
+        if (!rc) KCUDA(cudaStreamWaitEvent(h->stream, io->rho_ready, 0));
+        if (!rc) {
+            e = kk::launch_pdl(kk::k_advect_part<4>, nb_u, T, 0, h->stream, g, h->b, cu, 1 - cu, cr, 1 - cr, nb_u);
+            rc = launched("k_advect_part<4>", e);
+        }
+    } else if (!rc) {
+        rc = launch_advect(h, cu, 1 - cu, cr, 1 - cr);
+    }
     if (!rc && after_advect) KCUDA(cudaEventRecord(after_advect, h->stream));
     mark(1);
     if (!rc) rc = launch_geo(h, 1 - cu);
@@ -512,6 +538,7 @@ static int enqueue_step(kamino_solver_s* h, int cu, int cr, cudaEvent_t* ev, cud
                                        h->stream, g, h->b, cu, 1 - cu);
         rc = launched("k_ifft_u", e);
     }
+    if (!rc && io) KCUDA(cudaEventRecord(io->u_done, h->stream));
     mark(5);
     if (!rc) {
         const KGeo& g = h->g;
@@ -894,31 +921,62 @@ extern "C" int kamino_step_host(kamino_handle h, float dt, const float* u_phi_in
     if (pitch_bytes < w) return kamino_fail(KAMINO_ERR_INVALID, "pitch %zu < row bytes %zu", pitch_bytes, w);
     if (!h->io_stream) {
         KCUDA(cudaStreamCreateWithFlags(&h->io_stream, cudaStreamNonBlocking));
-        KCUDA(cudaEventCreateWithFlags(&h->ev_adv, cudaEventDisableTiming));
+        for (cudaEvent_t* e : {&h->ev_adv, &h->ev_uv, &h->ev_rho, &h->ev_u})
+            KCUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     }
     h->last_dt = dt;
     if ((rc = apply_dt(h, dt))) return rc;
-    if ((rc = copy_field(h, KAMINO_U_PHI, (void*)u_phi_in, pitch_bytes, true, cudaMemcpyHostToDevice, false)) ||
-        (rc = copy_field(h, KAMINO_U_THETA, (void*)u_theta_in, pitch_bytes, true, cudaMemcpyHostToDevice, false)) ||
-        (rc = copy_field(h, KAMINO_THICKNESS, (void*)thickness_in, pitch_bytes, true, cudaMemcpyHostToDevice,
-                         false)))
-        return rc;
+    const int rows = h->g.nt;
+    auto d2h = [&](float* dst, const float* src, int nrows) {
+        if (pitch_bytes == w) return cudaMemcpyAsync(dst, src, w * nrows, cudaMemcpyDeviceToHost, h->io_stream);
+        return cudaMemcpy2DAsync(dst, pitch_bytes, src, w, w, nrows, cudaMemcpyDeviceToHost, h->io_stream);
+    };
     const int cu = h->cur_uv, cr = h->cur_r;
-    if ((rc = enqueue_step(h, cu, cr, nullptr, h->ev_adv))) return rc;
-    h->cur_uv ^= 1;
-    h->cur_r ^= 1;
+    if (h->g.flags & KAMINO_F_REFERENCE_ROUNDING) {
+        // one advection launch: uploads, the step, and the thickness download
+        // overlapping the projection
+        if ((rc = copy_field(h, KAMINO_U_PHI, (void*)u_phi_in, pitch_bytes, true, cudaMemcpyHostToDevice, false)) ||
+            (rc = copy_field(h, KAMINO_U_THETA, (void*)u_theta_in, pitch_bytes, true, cudaMemcpyHostToDevice, false)) ||
+            (rc = copy_field(h, KAMINO_THICKNESS, (void*)thickness_in, pitch_bytes, true, cudaMemcpyHostToDevice,
+                             false)))
+            return rc;
+        if ((rc = enqueue_step(h, cu, cr, nullptr, h->ev_adv))) return rc;
+        KCUDA(cudaStreamWaitEvent(h->io_stream, h->ev_adv, 0));
+        KCUDA(d2h(thickness_out, h->b.rho[1 - cr], rows));
+        h->cur_uv ^= 1;
+        h->cur_r ^= 1;
+        if ((rc = copy_field(h, KAMINO_U_PHI, u_phi_out, pitch_bytes, false, cudaMemcpyDeviceToHost, false)) ||
+            (rc = copy_field(h, KAMINO_U_THETA, u_theta_out, pitch_bytes, false, cudaMemcpyDeviceToHost, false)))
+            return rc;
+    } else {
+        // u_phi and u_theta go up first and their advection starts while the
+        // thickness is still being copied in (on the second stream); the
+        // thickness comes back during the projection and u_phi during the
+        // u_theta gradient
+        if ((rc = copy_field(h, KAMINO_U_PHI, (void*)u_phi_in, pitch_bytes, true, cudaMemcpyHostToDevice, false)) ||
+            (rc = copy_field(h, KAMINO_U_THETA, (void*)u_theta_in, pitch_bytes, true, cudaMemcpyHostToDevice, false)))
+            return rc;
+        KCUDA(cudaEventRecord(h->ev_uv, h->stream));
+        KCUDA(cudaStreamWaitEvent(h->io_stream, h->ev_uv, 0));
+        if (pitch_bytes == w)
+            KCUDA(cudaMemcpyAsync(h->b.rho[cr], thickness_in, w * rows, cudaMemcpyHostToDevice, h->io_stream));
+        else
+            KCUDA(cudaMemcpy2DAsync(h->b.rho[cr], w, thickness_in, pitch_bytes, w, rows, cudaMemcpyHostToDevice,
+                                    h->io_stream));
+        KCUDA(cudaEventRecord(h->ev_rho, h->io_stream));
+        const HostIo io = {h->ev_rho, h->ev_u};
+        if ((rc = enqueue_step(h, cu, cr, nullptr, h->ev_adv, &io))) return rc;
+        KCUDA(cudaStreamWaitEvent(h->io_stream, h->ev_adv, 0));
+        KCUDA(d2h(thickness_out, h->b.rho[1 - cr], rows));
+        KCUDA(cudaStreamWaitEvent(h->io_stream, h->ev_u, 0));
+        KCUDA(d2h(u_phi_out, h->b.u[1 - cu], rows));
+        h->cur_uv ^= 1;
+        h->cur_r ^= 1;
+        if ((rc = copy_field(h, KAMINO_U_THETA, u_theta_out, pitch_bytes, false, cudaMemcpyDeviceToHost, false)))
+            return rc;
+    }
     h->steps++;
     h->time += h->g.dt;
-    const int rows = h->g.nt;
-    KCUDA(cudaStreamWaitEvent(h->io_stream, h->ev_adv, 0));
-    if (pitch_bytes == w)
-        KCUDA(cudaMemcpyAsync(thickness_out, h->b.rho[h->cur_r], w * rows, cudaMemcpyDeviceToHost, h->io_stream));
-    else
-        KCUDA(cudaMemcpy2DAsync(thickness_out, pitch_bytes, h->b.rho[h->cur_r], w, w, rows, cudaMemcpyDeviceToHost,
-                                h->io_stream));
-    if ((rc = copy_field(h, KAMINO_U_PHI, u_phi_out, pitch_bytes, false, cudaMemcpyDeviceToHost, false)) ||
-        (rc = copy_field(h, KAMINO_U_THETA, u_theta_out, pitch_bytes, false, cudaMemcpyDeviceToHost, false)))
-        return rc;
     KCUDA(cudaStreamSynchronize(h->io_stream));
     KCUDA(cudaStreamSynchronize(h->stream));
     return KAMINO_OK;

@@ -178,20 +178,28 @@ def test_fp64_mode_solves_agree(kg, orc, fp64_modes):
         assert orc.rel_l2(got[k], want[k]) <= TOL, (k, orc.rel_l2(got[k], want[k]))
 
 
-@pytest.mark.parametrize("nt", [64, 512])
-def test_step_host_matches_separate_calls_bitwise(kg, orc, nt):
-    """kamino_step_host (upload, step, download in one call, the thickness
-    download overlapping the projection) gives the bits of set_state x3,
-    kamino_step and get_state x3, over several steps."""
-    st = kg.make_initial_state(nt, lmax=8, seed=9)
-    cfg = kg.default_config(n_theta=nt, radius=1.0, dt=0.003)
+@pytest.mark.parametrize("nt,npart,ref", [(64, 0, False), (512, 0, False), (1024, 4096, False), (128, 1024, True)])
+def test_step_host_matches_separate_calls_bitwise(kg, orc, nt, npart, ref):
+    """kamino_step_host (upload, step, download in one call: the u_phi and
+    u_theta advection starts while the thickness is still being uploaded, the
+    thickness and u_phi downloads overlap the rest of the step) gives the
+    bits of set_state x3, kamino_step and get_state x3, over several steps;
+    particles, which stay on the device, too."""
+    st = kg.make_initial_state(nt, lmax=8, seed=9, n_particles=npart)
+    cfg = kg.default_config(n_theta=nt, radius=1.0, dt=0.003, n_particles=npart,
+                            flags=kg.F_REFERENCE_ROUNDING if ref else 0)
     with kg.KaminoSolver(config=cfg) as a, kg.KaminoSolver(config=cfg) as b:
         u, v, r = st["u_phi"], st["u_theta"], st["thickness"]
+        if npart:
+            a.set_state(kg.PARTICLES, st["particles"])
         b.load(st)
         for _ in range(3):
             u, v, r = a.step_host(u, v, r)
             b.stepForward()
         want = b.fields()
+        if npart:
+            assert np.array_equal(a.get_state(kg.PARTICLES), want["particles"])
+        assert a.time_elapsed() == b.time_elapsed()
     assert np.array_equal(u, want["u_phi"])
     assert np.array_equal(v, want["u_theta"])
     assert np.array_equal(r, want["thickness"])
