@@ -190,8 +190,9 @@ int kamino_init_fbm(kamino_handle h);
  * u_phi, u_theta and the thickness, KaminoSolver::stepForward(dt) and
  * copyBackToCPU of the three (KaminoQuantity.cu:3-18, KaminoSolver.cu:
  * 197-221) in one call, which returns when the outputs are in host memory.
- * The thickness download starts as soon as the advection has written it and
- * overlaps the rest of the step.  Same results as the separate calls; the
+ * The copies overlap the step: u_phi and u_theta are advected while the
+ * thickness is still being uploaded, and the thickness and u_phi downloads
+ * start as soon as each is final.  Same results as the separate calls; the
  * in and out buffers may be the same.  pitch_bytes: host row pitch (0 =
  * dense); pinned host memory (kamino_host_alloc) copies fastest. */
 int kamino_step_host(kamino_handle h, float dt, const float* u_phi_in, const float* u_theta_in,
