@@ -71,8 +71,8 @@ enum kamino_flags {
     /* Use the dt passed to kamino_step().  The reference ignores it and uses
      * the configured dt (KaminoSolver.cu:199, KaminoCore.cu:871). */
     KAMINO_F_HONOR_STEP_DT = 1u << 2,
-    /* Skip writing the pressure field (it is an intermediate of the step). */
-    KAMINO_F_NO_PRESSURE_OUT = 1u << 3,
+    /* 1u << 3 is reserved (the pressure is read back by the u_theta
+     * gradient, so a step always writes it). */
     /* Evaluate sample positions in radians with the reference's own
      * float/double rounding (KaminoCore.cu:11-52), so the pole-wrap index
      * map is bit-exact with the reference kernels.  Without this flag,

@@ -16,7 +16,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_IO, ERR_BUDGET, ERR_TIMEOUT, ERR_NOT_R
 U_PHI, U_THETA, THICKNESS, PRESSURE, PARTICLES = range(5)
 FRAME_GRID, FRAME_PARTICLES = range(2)
 # flags (enum kamino_flags)
-F_PARTICLE_RK2, F_POLE_SIGN_FLIP, F_HONOR_STEP_DT, F_NO_PRESSURE_OUT, F_REFERENCE_ROUNDING = 1, 2, 4, 8, 16
+F_PARTICLE_RK2, F_POLE_SIGN_FLIP, F_HONOR_STEP_DT, F_REFERENCE_ROUNDING = 1, 2, 4, 16
 
 
 class KaminoError(RuntimeError):

@@ -589,15 +589,28 @@ static int check_handle(kamino_solver_s* h)
     return KAMINO_OK;
 }
 
-// Rebuild dt-dependent tables when KAMINO_F_HONOR_STEP_DT asks for a new dt.
+// Rebuild dt-dependent tables when KAMINO_F_HONOR_STEP_DT asks for a new dt:
+// every table and constant kamino_create derives from the configured dt, so
+// the step equals that of a handle created with this dt.
 static int apply_dt(kamino_solver_s* h, float dt)
 {
     if (!(h->g.flags & KAMINO_F_HONOR_STEP_DT) || dt == h->g.dt) return KAMINO_OK;
     if (!(dt > 0) || !std::isfinite(dt)) return kamino_fail(KAMINO_ERR_INVALID, "dt=%g must be positive", dt);
+    const int nt = h->g.nt;
+    const double dtd = dt, R = h->cfg.radius, hd = KAMINO_PI_D / nt;
+    std::vector<float> cellc(nt), cellv(nt);
+    for (int j = 0; j < nt; j++) {  // as kamino_create
+        cellc[j] = (float)(dtd / (R * std::sin((j + 0.5) * hd) * hd));
+        cellv[j] = (float)(dtd / (R * std::sin((j + 1.0) * hd) * hd));
+    }
     h->g.dt = dt;
     h->g.cofTheta = dt / h->g.R;
-    kk::k_tables<<<(h->g.nt + 127) / 128, 128, 0, h->stream>>>(h->g, h->b);
+    h->g.cellTheta = (float)(dtd / (R * hd));
+    KCUDA(cudaMemcpyAsync(h->b.cell_c, cellc.data(), 4 * (size_t)nt, cudaMemcpyHostToDevice, h->stream));
+    KCUDA(cudaMemcpyAsync(h->b.cell_v, cellv.data(), 4 * (size_t)nt, cudaMemcpyHostToDevice, h->stream));
+    kk::k_tables<<<(nt + 127) / 128, 128, 0, h->stream>>>(h->g, h->b);
     KCUDA(cudaGetLastError());
+    KCUDA(cudaStreamSynchronize(h->stream));  // the host tables above go out of scope
     destroy_graphs(h);
     return KAMINO_OK;
 }

@@ -248,3 +248,44 @@ def test_fbm_velocity_init_vs_reference_arithmetic(kg, orc, nt):
         same = np.mean(got.view(np.uint32) == want.view(np.uint32))
         assert same >= 0.9999, same
         assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max()
+
+
+def test_honored_step_dt_equals_a_handle_created_with_that_dt(kg):
+    """KAMINO_F_HONOR_STEP_DT: kamino_step(dt') steps exactly like a handle
+    configured with dt' (every dt-derived table rebuilt); without the flag the
+    dt argument is ignored, as the reference's stepForward does
+    (KaminoSolver.cu:199, KaminoCore.cu:871)."""
+    nt = 128
+    st = kg.make_initial_state(nt, lmax=8, seed=31, n_particles=1024)
+    dt2 = float(np.float32(0.003))
+    mk = lambda dt, flags: kg.KaminoSolver(config=kg.default_config(n_theta=nt, radius=1.3, dt=dt, n_particles=1024,
+                                                                    flags=flags))
+    with mk(0.005, kg.F_HONOR_STEP_DT) as a, mk(dt2, 0) as b, mk(0.005, 0) as c, mk(0.005, 0) as d:
+        for s in (a, b, c, d):
+            s.load(st)
+        for _ in range(3):
+            a.stepForward(dt2)
+            b.stepForward()
+            c.stepForward(dt2)  # ignored without the flag
+            d.stepForward()
+        fa, fb, fc, fd = a.fields(), b.fields(), c.fields(), d.fields()
+    for k in ("u_phi", "u_theta", "thickness", "particles"):
+        assert np.array_equal(fa[k].view(np.uint32), fb[k].view(np.uint32)), k
+        assert np.array_equal(fc[k].view(np.uint32), fd[k].view(np.uint32)), k
+    assert not np.array_equal(fa["thickness"], fc["thickness"])
+
+
+@pytest.mark.parametrize("nt,steps", [(64, 1), (128, 20)])
+def test_pole_sign_flip_vs_fp64_oracle(kg, orc, nt, steps):
+    """KAMINO_F_POLE_SIGN_FLIP (u_phi / u_theta samples taken across a pole
+    are negated; the reference does not, KaminoCore.cu:43,52,93,102): the
+    step against the oracle run with the same switch."""
+    st, s, o = make_pair(kg, orc, nt, 0.005, flags=kg.F_POLE_SIGN_FLIP, npart=256)
+    s.step_n(steps)
+    o.step(steps)
+    got, want = s.fields(), o.fields()
+    s.close()
+    for k in FIELDS:
+        err = orc.rel_l2(got[k], want[k])
+        assert err <= TOL, "%s after %d steps with the pole sign flip: rel L2 %.3e" % (k, steps, err)
+    assert np.abs(got["particles"].astype(np.float64) - o.get_state(4)).max() < 1e-4
