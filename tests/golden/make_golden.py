@@ -5,7 +5,7 @@ come from running its kernels (KaminoGPU/kernel/KaminoCore.cu, tdm.cu,
 KaminoSolver.cu compiled unchanged into oracle/_ref/*.cubin) through the
 harness oracle/ref/kref_harness.cpp on a GB300:
 
-  python tests/golden/make_golden.py <out_dir>
+  python tests/golden/make_golden.py [out_dir]    (default: tests/golden/new/)
 
 ref_index.npz  index tuples and alphas of the reference samplers' index
                stage (its own validateCoord) for a fixed 20,000-point subset
@@ -83,4 +83,4 @@ def main(out):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "gpurun_out", "golden"))
+    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(os.path.dirname(os.path.abspath(__file__)), "new"))
