@@ -89,6 +89,11 @@ def test_frame_entry_points_reject_bad_arguments(kg):
     assert kg.lib.kamino_frame_write(None, kg.FRAME_GRID, None, None, 0) == kg.ERR_INVALID
     assert kg.lib.kamino_run_frames_bgeo(None, -1, None, None, None) == kg.ERR_INVALID
     assert kg.lib.kamino_frame_time_pack(None, kg.FRAME_GRID, 0, 0, None) == kg.ERR_INVALID
+    img = np.zeros((4, 4, 3), np.uint8)
+    assert kg.lib.kamino_init_density_image(None, img.ctypes.data, 4, 4, 12) == kg.ERR_INVALID
+    assert kg.lib.kamino_init_particle_colors_image(None, img.ctypes.data, 4, 4, 12) == kg.ERR_INVALID
+    assert kg.lib.kamino_init_particles(None, 1) == kg.ERR_INVALID
+    assert kg.lib.kamino_reference_particles(None, 1, None, 0) == kg.ERR_INVALID
 
 
 @pytest.mark.parametrize("density,nt,seed", [(1.0, 32, 1), (4.0, 64, 1), (2.0, 64, 7), (3.7, 32, 1)])

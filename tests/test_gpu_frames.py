@@ -222,3 +222,16 @@ def test_cli_reads_ppm_images(kg, orc, tmp_path):
     _, rec = orc.read_bgeo((tmp_path / "g_0.bgeo").read_bytes())
     assert np.array_equal(rec[:, 7], rho0.reshape(-1))
     assert np.array_equal(rho0, orc.image_density(orc.image_resample(dimg, 2 * nt, nt)))
+
+
+def test_image_arguments_are_checked(kg):
+    img = np.zeros((4, 5, 3), np.uint8)
+    cfg = kg.default_config(n_theta=32, radius=1.0, dt=0.005, n_particles=0)
+    with kg.KaminoSolver(config=cfg) as s:
+        for args in ((img.ctypes.data, 0, 4, 15), (img.ctypes.data, 5, 4, 14), (None, 5, 4, 15)):
+            assert kg.lib.kamino_init_density_image(s._h, *args) == kg.ERR_INVALID
+            assert "image" in kg._lib.last_error()
+        # no particles: nothing to colour, not an error
+        kg.check(kg.lib.kamino_init_particle_colors_image(s._h, img.ctypes.data, 5, 4, 15))
+        kg.check(kg.lib.kamino_init_density_image(s._h, img.ctypes.data, 5, 4, 15))
+        assert not s.get_state(kg.THICKNESS).any()
