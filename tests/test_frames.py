@@ -171,3 +171,20 @@ def test_oracle_image_resample(orc, w, h, dw, dh):
     assert (flat == 77).all()
     d = orc.image_density(got)
     assert d.shape == (dh, dw) and d.min() >= 0 and d.max() <= 1
+
+
+def test_cli_reports_unreadable_images(kg, tmp_path):
+    """The executable reads binary PPM images; anything else is reported and
+    ignored, as the reference ignores an image it cannot read
+    (KaminoSolver.cu:250-254, KaminoParticles.cu:8-11)."""
+    import os
+    import subprocess
+    exe = os.path.join(os.path.dirname(kg.LIB_PATH), "kamino")
+    (tmp_path / "d.png").write_bytes(b"\x89PNG\r\n\x1a\n not really")
+    (tmp_path / "bad.ppm").write_bytes(b"P6\n4 4\n65535\n" + bytes(96))
+    cfg = tmp_path / "configKamino.txt"
+    cfg.write_text("1.0 32 1.0 0.005 0.01 0 0.0 1 1 1 1 %s %s %s null %s\n"
+                   % (tmp_path / "g_", tmp_path / "p_", tmp_path / "d.png", tmp_path / "bad.ppm"))
+    r = subprocess.run([exe, str(cfg)], capture_output=True, text=True, timeout=120)
+    assert "density image '%s' ignored" % (tmp_path / "d.png") in r.stderr
+    assert "colour image '%s' ignored" % (tmp_path / "bad.ppm") in r.stderr
