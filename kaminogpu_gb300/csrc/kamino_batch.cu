@@ -471,14 +471,14 @@ static int batch_handle(kamino_batch b, int sphere, kamino_handle* h)
 
 extern "C" int kamino_batch_set_state(kamino_batch b, int sphere, int field, const float* host, size_t pitch_bytes)
 {
-    kamino_handle h;
+    kamino_handle h = nullptr;
     int rc = batch_handle(b, sphere, &h);
     return rc ? rc : kamino_set_state(h, field, host, pitch_bytes);
 }
 
 extern "C" int kamino_batch_get_state(kamino_batch b, int sphere, int field, float* host, size_t pitch_bytes)
 {
-    kamino_handle h;
+    kamino_handle h = nullptr;
     int rc = batch_handle(b, sphere, &h);
     return rc ? rc : kamino_get_state(h, field, host, pitch_bytes);
 }

@@ -463,7 +463,7 @@ extern "C" int kamino_frame_capture(kamino_handle h, int kind)
 {
     int rc = check_kind(kind);
     if (rc) return rc;
-    KFrames* f;
+    KFrames* f = nullptr;
     if ((rc = frame_state(h, &f))) return rc;
     return capture(h, f, kind);
 }
@@ -473,7 +473,7 @@ extern "C" int kamino_frame_write(kamino_handle h, int kind, const char* path, v
     int rc = check_kind(kind);
     if (rc) return rc;
     if (!path && !host) return kamino_fail(KAMINO_ERR_INVALID, "kamino_frame_write: no path and no buffer");
-    KFrames* f;
+    KFrames* f = nullptr;
     if ((rc = frame_state(h, &f))) return rc;
     return finish(h, f, kind, path, host, host_bytes);
 }
@@ -486,7 +486,7 @@ extern "C" int kamino_run_frames_bgeo(kamino_handle h, int frames, const char* g
                                       const char* particle_path, int64_t* steps_taken)
 {
     if (frames < 0) return kamino_fail(KAMINO_ERR_INVALID, "frames=%d < 0", frames);
-    KFrames* f;
+    KFrames* f = nullptr;
     int rc = frame_state(h, &f);
     if (rc) return rc;
     double dt = 0, DT = 0;
@@ -554,7 +554,7 @@ extern "C" int kamino_frame_time_pack(kamino_handle h, int kind, int reps, int f
     int rc = check_kind(kind);
     if (rc) return rc;
     if (reps < 1 || !ms) return kamino_fail(KAMINO_ERR_INVALID, "reps must be >= 1 and ms non-null");
-    KFrames* f;
+    KFrames* f = nullptr;
     if ((rc = frame_state(h, &f))) return rc;
     KGeo g;
     KBufs b;
@@ -671,7 +671,7 @@ int finish_image(kamino_handle h, int rc, void* scratch)
 // image: the thickness of every cell from the mirrored, resampled image.
 extern "C" int kamino_init_density_image(kamino_handle h, const uint8_t* bgr, int width, int height, size_t stride)
 {
-    KFrames* f;
+    KFrames* f = nullptr;
     int rc = frame_state(h, &f);  // makes the handle's device current
     if (rc) return rc;
     KBufs b;
@@ -688,7 +688,7 @@ extern "C" int kamino_init_density_image(kamino_handle h, const uint8_t* bgr, in
 extern "C" int kamino_init_particle_colors_image(kamino_handle h, const uint8_t* bgr, int width, int height,
                                                  size_t stride)
 {
-    KFrames* f;
+    KFrames* f = nullptr;
     int rc = frame_state(h, &f);
     if (rc) return rc;
     KGeo g;

@@ -622,7 +622,7 @@ extern "C" int kamino_step(kamino_handle h, float dt)
     h->last_dt = dt;  // stored, as stepForward does (KaminoSolver.cu:199)
     rc = apply_dt(h, dt);
     if (rc) return rc;
-    cudaGraphExec_t ge;
+    cudaGraphExec_t ge = nullptr;
     rc = get_graph(h, 1, &ge);
     if (rc) return rc;
     KCUDA(cudaGraphLaunch(ge, h->stream));
@@ -640,7 +640,7 @@ extern "C" int kamino_step_n(kamino_handle h, int n)
     if (n < 0) return kamino_fail(KAMINO_ERR_INVALID, "step count %d < 0", n);
     for (int k = 0; k < n;) {
         int s = (n - k >= 2) ? 2 : 1;
-        cudaGraphExec_t ge;
+        cudaGraphExec_t ge = nullptr;
         rc = get_graph(h, s, &ge);
         if (rc) return rc;
         KCUDA(cudaGraphLaunch(ge, h->stream));
@@ -872,7 +872,7 @@ static int copy_field(kamino_solver_s* h, int field, void* other, size_t pitch, 
     int rc = check_handle(h);
     if (rc) return rc;
     if (!other) return kamino_fail(KAMINO_ERR_INVALID, "null buffer");
-    int rows;
+    int rows = 0;
     rc = field_geometry(h, field, &rows);
     if (rc) return rc;
     float* d = field_dev(h, field);
