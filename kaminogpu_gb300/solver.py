@@ -147,6 +147,8 @@ class KaminoSolver:
         """The reference's FBM curl-noise velocity (kamino_init_fbm)."""
         check(lib.kamino_init_fbm(self._h))
 
+    initialize_velocity = init_fbm  # KaminoSolver::initialize_velocity, KaminoInitializer.cu:3-85
+
     def initParticlesfromPic(self, image=None, seed=1):
         """KaminoSolver::initParticlesfromPic: the reference's jittered
         particle placement (kamino_init_particles) and, given a decoded image
@@ -284,3 +286,61 @@ class KaminoSolver:
         cells = np.empty((phi.size, 2), np.int32)
         check(lib.kamino_probe_wrap(self._h, phi.ctypes.data, theta.ctypes.data, phi.size, cells.ctypes.data))
         return phi, theta, cells
+
+
+def read_ppm(path):
+    """A binary PPM (P6, maxval 255) as uint8 [height, width, 3] in B, G, R
+    order (the order the image entry points take, OpenCV's)."""
+    data = open(path, "rb").read()
+    fields, pos = [], 2
+    if data[:2] != b"P6":
+        raise ValueError("%s: not a binary PPM" % path)
+    while len(fields) < 3:
+        while pos < len(data) and (data[pos:pos + 1].isspace() or data[pos:pos + 1] == b"#"):
+            if data[pos:pos + 1] == b"#":
+                pos = data.index(b"\n", pos)
+            pos += 1
+        start = pos
+        while pos < len(data) and data[pos:pos + 1].isdigit():
+            pos += 1
+        fields.append(int(data[start:pos]))
+    w, h, maxval = fields
+    if maxval != 255:
+        raise ValueError("%s: only 8-bit PPM is supported" % path)
+    pix = np.frombuffer(data, np.uint8, w * h * 3, pos + 1).reshape(h, w, 3)
+    return np.ascontiguousarray(pix[..., ::-1])
+
+
+class Kamino:
+    """The reference's top-level driver (KaminoGPU/include/KaminoGPU.cuh:40-48,
+    Kamino::run at KaminoGPU/kernel/KaminoCore.cu:860-912) over the C ABI:
+    the solver with the FBM velocity, the density and colour images (binary
+    PPM here; the reference reads any format with OpenCV), the particle
+    placement, and the frame loop writing <gridPath><i>.bgeo and
+    <particlePath><i>.bgeo for frames 0 .. frames."""
+
+    def __init__(self, radius, nTheta, particleDensity, dt, DT, frames, A=0.0, B=1, C=1, D=1, E=1,
+                 gridPath="", particlePath="", densityImage="", solidImage="", colorImage="", **ext):
+        self.config = default_config(radius=radius, n_theta=nTheta, particle_density=particleDensity, dt=dt,
+                                     frame_dt=DT, frames=frames, A=A, B=B, C=C, D=D, E=E, grid_path=gridPath,
+                                     particle_path=particlePath, density_image=densityImage,
+                                     solid_image=solidImage, color_image=colorImage, n_particles=-1, **ext)
+
+    @classmethod
+    def from_config(cls, path, **ext):
+        """main(configKamino.txt) (KaminoGPU/kernel/main.cu:17-45)."""
+        k = cls.__new__(cls)
+        k.config = parse_config(path)
+        for a, v in ext.items():
+            setattr(k.config, a, v.encode() if isinstance(v, str) else v)
+        return k
+
+    def run(self):
+        """Kamino::run; returns the number of steps taken."""
+        c = self.config
+        with KaminoSolver(config=c) as s:
+            s.init_fbm()
+            if c.density_image:
+                s.initDensityfromPic(read_ppm(c.density_image.decode()))
+            s.initParticlesfromPic(read_ppm(c.color_image.decode()) if c.color_image else None)
+            return s.run_frames_bgeo(c.frames, c.grid_path.decode() or None, c.particle_path.decode() or None)

@@ -188,3 +188,19 @@ def test_cli_reports_unreadable_images(kg, tmp_path):
     r = subprocess.run([exe, str(cfg)], capture_output=True, text=True, timeout=120)
     assert "density image '%s' ignored" % (tmp_path / "d.png") in r.stderr
     assert "colour image '%s' ignored" % (tmp_path / "bad.ppm") in r.stderr
+
+
+def test_read_ppm_and_the_kamino_driver_config(kg, tmp_path):
+    rng = np.random.default_rng(8)
+    img = rng.integers(0, 256, (6, 9, 3), dtype=np.uint8)
+    p = tmp_path / "a.ppm"
+    p.write_bytes(b"P6\n# comment\n9 6\n255\n" + np.ascontiguousarray(img[..., ::-1]).tobytes())
+    assert np.array_equal(kg.read_ppm(p), img)
+    p.write_bytes(b"P6\n9 6\n65535\n" + bytes(9 * 6 * 6))
+    with pytest.raises(ValueError):
+        kg.read_ppm(p)
+    k = kg.Kamino(2.0, 64, 3.0, 0.004, 0.02, 7, gridPath="g_", particlePath="p_")
+    c = k.config
+    assert (c.radius, c.n_theta, c.dt, c.frame_dt, c.frames) == (2.0, 64, 0.004, 0.02, 7)
+    assert c.grid_path == b"g_" and c.particle_path == b"p_" and kg.particle_count(c) == 2 * int(np.float32(
+        np.sqrt(np.float32(3.0)) * 64)) ** 2

@@ -222,6 +222,11 @@ def test_cli_reads_ppm_images(kg, orc, tmp_path):
     _, rec = orc.read_bgeo((tmp_path / "g_0.bgeo").read_bytes())
     assert np.array_equal(rec[:, 7], rho0.reshape(-1))
     assert np.array_equal(rho0, orc.image_density(orc.image_resample(dimg, 2 * nt, nt)))
+    # the Python mirror of Kamino::run writes the same files
+    kg.Kamino.from_config(cfgfile, grid_path=str(tmp_path / "kg_"), particle_path=str(tmp_path / "kp_")).run()
+    for i in range(frames + 1):
+        assert (tmp_path / ("kg_%d.bgeo" % i)).read_bytes() == (tmp_path / ("g_%d.bgeo" % i)).read_bytes(), i
+        assert (tmp_path / ("kp_%d.bgeo" % i)).read_bytes() == (tmp_path / ("p_%d.bgeo" % i)).read_bytes(), i
 
 
 def test_image_arguments_are_checked(kg):
