@@ -16,8 +16,12 @@ e2e:   the same steps through the public C ABI with host buffers: every step
   download overlapping the projection).
 --impl reference: the reference has no CPU implementation of this path, so
   the reference arm times the CPU port of its step (oracle/, FP64, all host
-  threads) on the same configuration, plus the reference's own CUDA kernels
-  on this GPU as extra information.
+  threads) on the same configuration, from the same seeded state made by the
+  oracle's own generator (the product library is never loaded there), plus
+  the reference's own CUDA kernels on this GPU as extra information.
+Extra keys of the GPU arm: config2 (nTheta=512 with 2^20 RK2 particles),
+  batched (256 spheres), served (closed loop, and Poisson arrivals at 200/s
+  for --served-seconds, 60 by default), frame_output, cpu_baseline.
 With N > 1 (torchrun), every rank advances its own sphere (replicas; the
 path does not shard) and rank 0 prints the aggregate.
 """
@@ -37,6 +41,18 @@ NT, DT, LMAX, SEED = 1024, 0.001, 32, 1
 METRIC = "cell-steps/s at 1024x2048, batched/served vs plain; p99 latency @1e-5 rel err"
 UNIT = "cell-steps/s"
 STEP_BYTES_PER_CELL = 56    # algorithmic bytes per cell-step of the whole step (3-pass minimum)
+PARTICLE_BYTES = 16         # algorithmic bytes per particle-step: (phi, theta) read and written
+DATA = ("synthetic: seeded l<=32 spherical-harmonic stream function + Gaussian vortex (sigma 0.1 rad), "
+        "max|u|=1; thickness 1+0.05U(-1,1)")
+
+
+def workload_config(ws):
+    """The `config` both arms print: the workload only, nothing arm-specific."""
+    return {"workload": "plain solver, one sphere nTheta=1024 nPhi=2048, radius 1, dt=0.001 (precision form)",
+            "n_theta": NT, "n_phi": 2 * NT, "radius": 1.0, "dt": DT, "lmax": LMAX, "vortex_sigma": 0.1,
+            "seed": SEED, "fp64_modes": 4,
+            "l2": "GPU arm: a 256 MiB buffer written then read before every timed step (cold, clean L2)",
+            "parallelism": "replicas" if ws > 1 else "single GPU"}
 
 
 def dist_env():
@@ -238,11 +254,9 @@ def run_ours(args, ws, rank, local, dist):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32 (FP64 for Fourier modes |m|<=4)",
-        "data": "synthetic: seeded l<=32 spherical-harmonic stream function + Gaussian vortex (sigma 0.1 rad), "
-                "max|u|=1; thickness 1+0.05U(-1,1)",
-        "config": {"workload": "plain solver, one sphere nTheta=1024 nPhi=2048, radius 1, dt=0.001 (precision form)",
-                   "sampler": "cell-exact", "fp64_modes": 4, "l2": "256 MiB buffer written then read before every timed step (cold, clean L2)",
-                   "parallelism": "replicas" if ws > 1 else "single GPU", "wall_s_timed_region": wall},
+        "data": DATA,
+        "config": workload_config(ws),
+        "implementation": {"sampler": "cell-exact", "wall_s_timed_region": wall},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": sum(nbytes.values()),
                 "d2h_bytes_per_step": sum(nbytes.values())},
         "gpu_launches": launches * args.steps,
@@ -256,6 +270,8 @@ def run_ours(args, ws, rank, local, dist):
         "dominant_kernel": dom,
         "clocks": ck.summary(),
     }
+    if not args.no_config2:
+        out["config2"] = bench_particles(kg, local, hbm)
     if not args.no_batched:
         out["batched"] = bench_batched(kg, local)
     if not args.no_served:
@@ -265,6 +281,45 @@ def run_ours(args, ws, rank, local, dist):
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(st, seconds=10.0)
     return out
+
+
+def bench_particles(kg, local, hbm, npart=1 << 20, steps=200):
+    """The mid-size configuration with particles: nTheta=512, nPhi=1024,
+    radius 1, dt=0.002, l<=16, 2^20 particles uniform on the sphere advected
+    with RK2 every step.  Device time per step, and the particles' share of
+    the advection launch (k_advect with and without the particle tiles) with
+    its roofline at 16 B per particle-step."""
+    nt = 512
+    st = kg.make_initial_state(nt, lmax=16, seed=SEED, n_particles=npart)
+    res = {}
+    for n in (npart, 0):
+        cfg = kg.default_config(n_theta=nt, radius=1.0, dt=0.002, n_particles=n, flags=kg.F_PARTICLE_RK2,
+                                fp64_modes=4, device=local)
+        with kg.KaminoSolver(config=cfg) as s:
+            s.load(st)
+            s.step_n(5)
+            s.synchronize()
+            kms = s.time_kernels(reps=10, flush_l2=True)
+            s.load(st)
+            s.step_n(3)
+            s.synchronize()
+            ms = s.time_steps(steps, flush_l2=True)
+        res[n] = (ms / steps, kms)
+    step_ms, kms = res[npart]
+    adv_p, adv_0 = kms["k_advect"], res[0][1]["k_advect"]
+    part_ms = max(adv_p - adv_0, 1e-9)
+    achieved = PARTICLE_BYTES * npart / (part_ms / 1e3) / 1e9
+    C = nt * 2 * nt
+    return {"workload": "nTheta=512 nPhi=1024, radius 1, dt=0.002, l<=16, 2^20 particles uniform on the sphere, "
+                        "RK2 particle advection, fp64_modes=4, %d timed steps (cold L2 each)" % steps,
+            "ms_per_step": step_ms, "cell_steps_per_s": C / (step_ms / 1e3),
+            "ms_per_step_without_particles": res[0][0],
+            "k_advect_ms": adv_p, "k_advect_ms_without_particles": adv_0,
+            "particle_share_of_k_advect": part_ms / adv_p,
+            "particle_roofline": {"bytes_per_particle_step": PARTICLE_BYTES, "achieved": achieved, "peak": hbm,
+                                  "frac": achieved / hbm, "unit": "GB/s",
+                                  "what": "16 B x 2^20 over the particle tiles' share of the k_advect launch"},
+            "kernel_ms": kms}
 
 
 def bench_frames(kg, local, st, hbm, frames=5, steps_per_frame=10):
@@ -548,23 +603,26 @@ def cpu_baseline(st, seconds=10.0):
 
 
 def run_reference(args, ws, rank):
-    import kaminogpu_gb300 as kg
+    """The reference arm: the CPU port of the reference step (oracle/, FP64,
+    all host threads) on the same workload, built from the same seeded state
+    by the oracle's own generator -- nothing of the product library is
+    loaded.  Same warm-up count as the GPU arm; the timed steps are a bounded
+    sample (about 30 s of CPU work at most)."""
     if rank != 0:
         return None
-    st = kg.make_initial_state(NT, lmax=LMAX, seed=SEED, vortex=True)
     from oracle import oracle as orc
+    st = orc.make_initial_state(NT, lmax=LMAX, seed=SEED, vortex=True)
     cores = orc.set_threads(os.cpu_count() or 1)
     o = orc.Oracle(NT, 1.0, DT)
     o.load(st)
     t0 = time.perf_counter()
-    o.step(1)  # warm-up
-    t1 = time.perf_counter() - t0
-    # a bounded sample: at most about 30 s of CPU work
+    o.step(args.warmup)
+    t1 = (time.perf_counter() - t0) / args.warmup
     n = int(max(1, min(args.steps, 30.0 / max(t1, 1e-3))))
     t0 = time.perf_counter()
     o.step(n)
     dt = time.perf_counter() - t0
-    args.steps = n
+    o.close()
     value = NT * 2 * NT * n / dt
     out = {
         "impl": "reference",
@@ -572,18 +630,20 @@ def run_reference(args, ws, rank):
         "value": value,
         "unit": UNIT,
         "n_gpus": ws,
-        "steps": args.steps,
-        "warmup": 1,
-        "ms_per_step": dt / args.steps * 1e3,
+        "steps": n,
+        "warmup": args.warmup,
+        "ms_per_step": dt / n * 1e3,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": "synthetic: same seeded state as the ours arm",
-        "config": {"workload": "plain solver, one sphere nTheta=1024 nPhi=2048, radius 1, dt=0.001 (precision form)",
-                   "implementation": "CPU port of the reference step (oracle/kamino_oracle.c), OpenMP"},
+        "data": DATA,
+        "config": workload_config(ws),
+        "implementation": {"what": "CPU port of the reference step (oracle/kamino_oracle.c), FP64, OpenMP",
+                           "steps_requested": args.steps},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": "%d FP64 steps of the nTheta=1024 sphere" % args.steps},
+                         "sample": "%d FP64 steps of the nTheta=1024 sphere after %d untimed (%.1f s)"
+                                   % (n, args.warmup, dt)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     if orc.have_reference_gpu():
@@ -614,7 +674,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-frames", action="store_true")
-    ap.add_argument("--served-seconds", type=float, default=5.0)
+    ap.add_argument("--no-config2", action="store_true")
+    ap.add_argument("--served-seconds", type=float, default=60.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -228,7 +228,11 @@ int kamino_projection(kamino_handle h);
  * inputs); every pointer 16-byte aligned.  stream is a cudaStream_t (NULL: the default stream); the call is
  * asynchronous on it.  The first call on a device looks up the array's
  * device address, so make it before any stream capture on that device.  All
- * calls share the array: calls whose work overlaps on the GPU race. */
+ * calls share the array, which keeps the tables of the last n_theta called
+ * and the last call's temporaries: calls whose work overlaps on the GPU race.
+ * A call with an n_theta other than the previous call's uploads that size's
+ * tables from host memory; on a stream that is capturing, such a call is
+ * refused with KAMINO_ERR_INVALID. */
 int kamino_projection_noalloc(int n_theta, const float* u_phi, const float* u_theta, float* u_phi_out,
                               float* u_theta_out, float* pressure_out, void* stream);
 
@@ -289,7 +293,8 @@ int kamino_frame_time_pack(kamino_handle h, int kind, int reps, int flush_l2, do
  * are write-only).  kamino_save_state writes u_phi, u_theta, the thickness,
  * the particles, the step count and the elapsed time to a file with a
  * checksum; kamino_load_state restores them into a handle of the same
- * n_theta, particle count, radius and dt (KAMINO_ERR_INVALID otherwise;
+ * n_theta, particle count, radius, dt and trajectory flags (particle RK2,
+ * pole sign flip, honoured step dt, reference rounding; KAMINO_ERR_INVALID otherwise;
  * KAMINO_ERR_IO for a truncated or corrupted file).  Synchronous. */
 int kamino_save_state(kamino_handle h, const char* path);
 int kamino_load_state(kamino_handle h, const char* path);

@@ -525,6 +525,12 @@ extern "C" int kamino_load_state(kamino_handle h, const char* path)
     if (hd.radius != cfg.radius || hd.dt != cfg.dt)
         return kamino_fail(KAMINO_ERR_INVALID, "%s: radius %g, dt %g; the handle has radius %g, dt %g", path,
                            hd.radius, hd.dt, cfg.radius, cfg.dt);
+    // the switches that change the trajectory must match too
+    const uint32_t traj = KAMINO_F_PARTICLE_RK2 | KAMINO_F_POLE_SIGN_FLIP | KAMINO_F_HONOR_STEP_DT |
+                          KAMINO_F_REFERENCE_ROUNDING;
+    if ((hd.flags & traj) != (cfg.flags & traj))
+        return kamino_fail(KAMINO_ERR_INVALID, "%s: saved with flags 0x%x; the handle has 0x%x", path,
+                           hd.flags & traj, cfg.flags & traj);
     const float* p = data.data();
     if ((rc = kamino_set_state(h, KAMINO_U_PHI, p, 0)) || (rc = kamino_set_state(h, KAMINO_U_THETA, p + np * nt, 0)) ||
         (rc = kamino_set_state(h, KAMINO_THICKNESS, p + np * (2 * nt - 1), 0)))

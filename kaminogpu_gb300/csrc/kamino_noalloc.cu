@@ -167,6 +167,22 @@ extern "C" int kamino_projection_noalloc(int n_theta, const float* u_phi, const 
         if (carve((char*)slot.base, nt, &b) > NOALLOC_BYTES)
             return kamino_fail(KAMINO_ERR_INVALID, "kamino_projection_noalloc: scratch too small for n_theta=%d", nt);
         if (slot.nt_loaded != nt) {
+            // A table upload copies from host vectors that are freed when
+            // this call returns, so it must run now, not be recorded.
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            e = cudaStreamIsCapturing(stream, &cs);
+            if (e != cudaSuccess)
+                return kamino_fail(KAMINO_ERR_CUDA, "kamino_projection_noalloc: cudaStreamIsCapturing: %s",
+                                   cudaGetErrorString(e));
+            if (cs != cudaStreamCaptureStatusNone)
+                return kamino_fail(KAMINO_ERR_INVALID,
+                                   "kamino_projection_noalloc: the tables of n_theta=%d are not loaded and cannot "
+                                   "be loaded while the stream is capturing; call once with this n_theta outside "
+                                   "the capture first",
+                                   nt);
+            // the array holds no complete set of tables until the upload has
+            // been queued in full: a failure part-way leaves nothing to reuse
+            slot.nt_loaded = 0;
             int rc = load_tables(nt, g, b, stream);
             if (rc) return rc;
             slot.nt_loaded = nt;

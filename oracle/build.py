@@ -17,7 +17,20 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REFOUT = os.path.join(HERE, "_ref")
-REFSRC = os.environ.get("KAMINO_REFERENCE", "/root/reference")
+
+
+def _reference_tree():
+    """The reference checkout (Uchanka/KaminoGPU): $KAMINO_REFERENCE, else a
+    directory named `reference` beside this repository's root; None when
+    neither exists (the prebuilt reference artefacts are used as they are)."""
+    env = os.environ.get("KAMINO_REFERENCE")
+    if env:
+        return env
+    sib = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+    return sib if os.path.isdir(os.path.join(sib, "KaminoGPU")) else None
+
+
+REFSRC = _reference_tree()
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -35,16 +48,18 @@ def _stale(out, *srcs):
 
 def build_oracle():
     os.makedirs(BUILD, exist_ok=True)
-    src = os.path.join(HERE, "kamino_oracle.c")
+    srcs = [os.path.join(HERE, "kamino_oracle.c"), os.path.join(HERE, "synth_state.c")]
     out = os.path.join(BUILD, "libkamino_oracle.so")
-    if _stale(out, src):
+    if _stale(out, *srcs):
         _run(["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c11",
-              "-o", out, src, "-lm"])
+              "-o", out, *srcs, "-lm"])
     return out
 
 
 def build_ref_cubins():
     """Compile the reference kernels; returns False where the tree is absent."""
+    if REFSRC is None:
+        return False
     kdir = os.path.join(REFSRC, "KaminoGPU", "kernel")
     if not os.path.isdir(kdir):
         return False

@@ -58,8 +58,28 @@ def _oracle_lib():
         L.oracle_ref_particles.argtypes = [_F, _I, ctypes.c_uint, _P]
         L.oracle_ref_particles.restype = _I64
         L.oracle_image_resample.argtypes = [_P, _I, _I, ctypes.c_size_t, _I, _I, _P]
+        L.oracle_make_initial_state.argtypes = [_I, _I, ctypes.c_uint64, _D, _D, _I, _D, _D, _D, _I64,
+                                                _P, _P, _P, _P, _P]
+        L.oracle_make_initial_state.restype = _I
         _olib = L
     return _olib
+
+
+def make_initial_state(nt, lmax=8, seed=1, radius=1.0, thickness_noise=0.05, vortex=False, vortex_sigma=0.1,
+                       velocity_scale=1.0, n_particles=0):
+    """The seeded synthetic state of kamino_make_initial_state, made on the
+    CPU side (synth_state.c) without the product library; same dict."""
+    u = np.empty((nt, 2 * nt), np.float32)
+    v = np.empty((nt - 1, 2 * nt), np.float32)
+    rho = np.empty((nt, 2 * nt), np.float32)
+    part = np.empty((max(n_particles, 1), 2), np.float32)
+    vo = np.zeros(3, np.float64)
+    rc = _oracle_lib().oracle_make_initial_state(nt, lmax, seed, radius, thickness_noise, int(bool(vortex)),
+                                                 vortex_sigma, 0.0, velocity_scale, n_particles, u.ctypes.data,
+                                                 v.ctypes.data, rho.ctypes.data, part.ctypes.data, vo.ctypes.data)
+    if rc:
+        raise ValueError("oracle_make_initial_state(nt=%d, lmax=%d) failed" % (nt, lmax))
+    return {"u_phi": u, "u_theta": v, "thickness": rho, "particles": part[:n_particles], "vortex": tuple(vo)}
 
 
 def set_threads(n):

@@ -7,8 +7,8 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def solver(kg, nt=64, npart=512, dt=0.005, radius=1.0):
-    cfg = kg.default_config(n_theta=nt, radius=radius, dt=dt, n_particles=npart)
+def solver(kg, nt=64, npart=512, dt=0.005, radius=1.0, flags=0):
+    cfg = kg.default_config(n_theta=nt, radius=radius, dt=dt, n_particles=npart, flags=flags)
     return kg.KaminoSolver(config=cfg)
 
 
@@ -57,3 +57,8 @@ def test_damaged_and_mismatched_files_are_refused(kg, tmp_path):
         with pytest.raises(kg.KaminoError) as e:
             d.load_state(path)
         assert e.value.code == kg.ERR_INVALID and "dt" in str(e.value)
+    for flags in (kg.F_REFERENCE_ROUNDING, kg.F_PARTICLE_RK2):
+        with solver(kg, flags=flags) as f:
+            with pytest.raises(kg.KaminoError) as e:
+                f.load_state(path)
+            assert e.value.code == kg.ERR_INVALID and "flags" in str(e.value)

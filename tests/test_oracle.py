@@ -196,3 +196,15 @@ def test_fbm_init_restatements_agree(orc):
     assert np.array_equal(u.view(np.uint32), pu.view(np.uint32))
     assert np.array_equal(v.view(np.uint32), pv.view(np.uint32))
     assert np.abs(u).max() > 0 and np.abs(v).max() > 0
+
+
+@pytest.mark.parametrize("nt,lmax,vortex,npart", [(32, 8, False, 1000), (256, 16, True, 0), (1024, 32, True, 64)])
+def test_oracle_state_generator_matches_the_library(kg, orc, nt, lmax, vortex, npart):
+    """The benchmark's CPU arm builds its input with the oracle's copy of the
+    seeded state generator (so it never loads the product library); it must
+    be the library's state bit for bit."""
+    a = orc.make_initial_state(nt, lmax=lmax, seed=3, vortex=vortex, n_particles=npart, radius=1.3)
+    b = kg.make_initial_state(nt, lmax=lmax, seed=3, vortex=vortex, n_particles=npart, radius=1.3)
+    for k in ("u_phi", "u_theta", "thickness", "particles"):
+        assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), k
+    assert a["vortex"] == b["vortex"]
