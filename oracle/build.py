@@ -86,6 +86,32 @@ def build_ref_cubins():
     return True
 
 
+def build_ref_fbm():
+    """The reference's FBM velocity initialiser (KaminoInitializer.cu and
+    vectorUtil.cu, host C++, compiled unchanged) with ref/fbm_harness.cpp into
+    _ref/libref_fbm.so, for the golden vectors of tests/golden/make_golden.py.
+    Only where the reference tree exists; returns the path or None."""
+    if REFSRC is None:
+        return None
+    kg = os.path.join(REFSRC, "KaminoGPU")
+    kdir = os.path.join(kg, "kernel")
+    if not os.path.isdir(kdir):
+        return None
+    os.makedirs(REFOUT, exist_ok=True)
+    harness = os.path.join(HERE, "ref", "fbm_harness.cpp")
+    srcs = [os.path.join(kdir, "KaminoInitializer.cu"), os.path.join(kdir, "vectorUtil.cu")]
+    out = os.path.join(REFOUT, "libref_fbm.so")
+    if _stale(out, harness, *srcs):
+        inc = ["-I" + os.path.join(HERE, "ref", "shim"), "-I" + os.path.join(kg, "include"),
+               "-I" + os.path.join(kg, "cuda_util_headers"), "-I" + os.path.join(kg, "partio_headers"),
+               "-I" + os.path.join(kg, "opencv_headers"), "-I" + os.path.join(CUDA, "include")]
+        # no contraction into fused multiply-adds: the reference's own build
+        # (MSVC, x86) evaluates every product and sum separately
+        _run(["g++", "-O2", "-std=c++14", "-ffp-contract=off", "-fPIC", "-shared", "-w", *inc, "-o", out, harness,
+              "-x", "c++", *srcs])
+    return out
+
+
 def have_ref_cubins():
     return all(os.path.exists(os.path.join(REFOUT, n))
                for n in ("ref_core.cubin", "ref_tdm.cubin", "ref_solver.cubin"))

@@ -16,14 +16,23 @@ FIELDS = ("u_phi", "u_theta", "thickness")
 TOL = 1e-5  # relative L2 per field against the FP64 oracle
 
 
-def make_pair(kg, orc, nt, dt, lmax=8, seed=3, npart=0, flags=0, vortex=False, fp64_modes=4):
-    st = kg.make_initial_state(nt, lmax=lmax, seed=seed, n_particles=npart, vortex=vortex)
-    cfg = kg.default_config(n_theta=nt, radius=1.0, dt=dt, n_particles=npart, flags=flags, fp64_modes=fp64_modes)
+def make_pair(kg, orc, nt, dt, lmax=8, seed=3, npart=0, flags=0, vortex=False, fp64_modes=4, radius=1.0):
+    st = kg.make_initial_state(nt, lmax=lmax, seed=seed, n_particles=npart, vortex=vortex, radius=radius)
+    cfg = kg.default_config(n_theta=nt, radius=radius, dt=dt, n_particles=npart, flags=flags, fp64_modes=fp64_modes)
     s = kg.KaminoSolver(config=cfg)
     s.load(st)
-    o = orc.Oracle(nt, 1.0, dt, flags & 3, npart)
+    o = orc.Oracle(nt, radius, dt, flags & 3, npart)
     o.load(st)
     return st, s, o
+
+
+def chord(p, q):
+    """Distance on the unit sphere between particle positions (phi, theta):
+    near a pole a small displacement can change phi by a lot."""
+    def xyz(a):
+        a = np.asarray(a, np.float64)
+        return np.stack([np.sin(a[:, 1]) * np.cos(a[:, 0]), np.sin(a[:, 1]) * np.sin(a[:, 0]), np.cos(a[:, 1])], 1)
+    return np.linalg.norm(xyz(p) - xyz(q), axis=1)
 
 
 @pytest.mark.parametrize("nt", [32, 128, 1024])
@@ -39,18 +48,76 @@ def test_stage_vs_fp64_oracle(kg, orc, nt, stage):
         assert err <= TOL, "%s after %s: rel L2 %.3e" % (k, stage, err)
 
 
-@pytest.mark.parametrize("nt,dt,steps,lmax", [(32, 0.005, 1, 8), (32, 0.005, 100, 8), (128, 0.005, 1, 8),
-                                              (128, 0.005, 100, 8), (256, 0.002, 100, 16),
-                                              (1024, 0.001, 1, 32), (2048, 0.0005, 1, 32)])
-def test_step_vs_fp64_oracle(kg, orc, nt, dt, steps, lmax):
-    st, s, o = make_pair(kg, orc, nt, dt, lmax=lmax, vortex=nt >= 1024)
+@pytest.mark.parametrize("nt,dt,steps,lmax,radius", [(32, 0.005, 1, 8, 1.0), (32, 0.005, 100, 8, 1.0),
+                                                     (128, 0.005, 1, 8, 1.0), (128, 0.005, 100, 8, 1.0),
+                                                     (256, 0.002, 100, 16, 1.0), (1024, 0.001, 1, 32, 1.0),
+                                                     (1024, 0.001, 100, 32, 1.0), (2048, 0.0005, 1, 32, 1.0),
+                                                     (64, 0.005, 100, 8, 0.5), (64, 0.005, 100, 8, 1.9),
+                                                     (256, 0.002, 100, 16, 0.5), (256, 0.002, 100, 16, 1.9)])
+def test_step_vs_fp64_oracle(kg, orc, nt, dt, steps, lmax, radius):
+    """Whole steps against the FP64 oracle: relative L2 <= 1e-5 per field
+    after 1 and 100 steps, at the precision-form size (nTheta = 1024, dt =
+    0.001, l <= 32 plus a vortex) and at the batched mix's radii."""
+    st, s, o = make_pair(kg, orc, nt, dt, lmax=lmax, vortex=nt >= 1024, radius=radius)
     s.step_n(steps)
     o.step(steps)
     got, want = s.fields(), o.fields()
     s.close()
     for k in FIELDS:
         err = orc.rel_l2(got[k], want[k])
-        assert err <= TOL, "%s after %d steps (nt=%d): rel L2 %.3e" % (k, steps, nt, err)
+        assert err <= TOL, "%s after %d steps (nt=%d, R=%g): rel L2 %.3e" % (k, steps, nt, radius, err)
+
+
+def _banded(a, b, cut):
+    """Relative L2 over the rows at least `cut` rows from either pole."""
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    sl = slice(cut, a.shape[0] - cut)
+    return np.linalg.norm(a[sl] - b[sl]) / np.linalg.norm(b[sl])
+
+
+def test_precision_form_200_steps(kg, orc):
+    """The precision-form workload as configured: nTheta = 1024, dt = 0.001,
+    200 steps, l <= 32 plus a vortex, FP64 for |m| <= 4.
+
+    The reference's samplers do not negate a vector sampled across a pole
+    (KaminoCore.cu:43-52, 93-102), so on the rows next to a pole the sample
+    jumps from u(phi) to u(phi + pi) ~ -u(phi) as a departure point crosses
+    theta = 0: the step is discontinuous there.  Two runs that differ at the
+    1e-7 level end up on opposite sides of that jump somewhere after about a
+    hundred steps, and the difference then spreads from the pole rows.  The
+    FP64 oracle does it to itself: started from this solver's state after 100
+    steps (5e-7 away), it is more than 1e-5 from the unperturbed FP64 run at
+    step 200.  So after 200 steps the test holds the fields to 1e-5 away from
+    the polar caps (32 rows, 5.6 degrees, from each pole), and with
+    KAMINO_F_POLE_SIGN_FLIP (the sampler made continuous across the pole) to
+    1e-5 on the whole sphere."""
+    nt, dt = 1024, 0.001
+    st, s, o = make_pair(kg, orc, nt, dt, lmax=32, vortex=True)
+    s.step_n(100)
+    o.step(100)
+    mid = s.fields()
+    b = orc.Oracle(nt, 1.0, dt, 0, 0)
+    b.load({k: mid[k] for k in FIELDS})
+    s.step_n(100)
+    o.step(100)
+    b.step(100)
+    got, want, pert = s.fields(), o.fields(), b.fields()
+    s.close()
+    b.close()
+    for k in FIELDS:
+        err = _banded(got[k], want[k], 32)
+        assert err <= TOL, "%s after 200 steps away from the poles: rel L2 %.3e" % (k, err)
+    # the FP64 oracle perturbed by this solver's 100-step error leaves the
+    # 1e-5 band by itself: the jump, not FP32 arithmetic, sets the error
+    assert max(orc.rel_l2(pert[k], want[k]) for k in ("u_phi", "u_theta")) > TOL
+    st, s, o = make_pair(kg, orc, nt, dt, lmax=32, vortex=True, flags=kg.F_POLE_SIGN_FLIP)
+    s.step_n(200)
+    o.step(200)
+    got, want = s.fields(), o.fields()
+    s.close()
+    for k in FIELDS:
+        err = orc.rel_l2(got[k], want[k])
+        assert err <= TOL, "%s after 200 steps with the pole sign flip: rel L2 %.3e" % (k, err)
 
 
 @pytest.mark.parametrize("nt,shift", [(256, 37), (2048, 1001), (2048, 2048)])
@@ -100,12 +167,17 @@ def test_stages_compose_to_step_bitwise(kg, orc, flags):
         assert np.array_equal(fa[k].view(np.uint32), fb[k].view(np.uint32)), k
 
 
-@pytest.mark.parametrize("nt", [32, 128])
+@pytest.mark.parametrize("nt", [32, 128, 1024])
 def test_reference_rounding_step_vs_reference_kernels(kg, orc, nt):
+    """KAMINO_F_REFERENCE_ROUNDING against the reference's own kernels, one
+    step.  At nTheta = 1024 the reference's FP32 cyclic reduction leaves
+    u_phi about 10% from FP64 and a divergence ~1000x the FP64 one, so there
+    the divergence check is one-sided (ours at most 2x the reference's)."""
     if not orc.have_reference_gpu():
         pytest.skip("reference cubins not built")
-    dt = 0.005
-    st, s, o = make_pair(kg, orc, nt, dt, npart=1024, flags=kg.F_REFERENCE_ROUNDING)
+    dt = 0.005 if nt < 1024 else 0.001
+    lmax = 8 if nt < 1024 else 32
+    st, s, o = make_pair(kg, orc, nt, dt, lmax=lmax, npart=1024, flags=kg.F_REFERENCE_ROUNDING, vortex=nt >= 1024)
     ref = orc.RefGPU(nt, 1.0, dt, 1024)
     ref.load(st)
     s.stepForward()
@@ -117,12 +189,16 @@ def test_reference_rounding_step_vs_reference_kernels(kg, orc, nt):
     for k in FIELDS:
         e_ours = orc.rel_l2(got[k], want[k])
         e_ref = orc.rel_l2(rf[k], want[k])
-        # never worse than the reference's own FP32 error against FP64
-        assert e_ours <= max(e_ref, TOL), "%s: ours %.3e, reference %.3e" % (k, e_ours, e_ref)
+        # never worse than the reference's own FP32 error against FP64 (to
+        # 0.1% of it: where both take the same branches they agree to FP32
+        # rounding, e.g. 3.95208e-5 against 3.95207e-5)
+        assert e_ours <= max(1.001 * e_ref, TOL), "%s: ours %.3e, reference %.3e" % (k, e_ours, e_ref)
     # post-projection divergence within 2x of the reference's
     d_ours = np.linalg.norm(o.divergence(got["u_phi"], got["u_theta"]))
     d_ref = np.linalg.norm(o.divergence(rf["u_phi"], rf["u_theta"]))
-    assert 0.5 <= d_ours / d_ref <= 2.0, (d_ours, d_ref)
+    assert d_ours / d_ref <= 2.0, (d_ours, d_ref)
+    if nt < 1024:
+        assert d_ours / d_ref >= 0.5, (d_ours, d_ref)
     # particles: the same forward-Euler update (KaminoCore.cu:321-342)
     dp = np.abs(got["particles"].astype(np.float64) - rf["particles"]).max()
     assert dp < 1e-5, dp
@@ -206,22 +282,28 @@ def test_step_host_matches_separate_calls_bitwise(kg, orc, nt, npart, ref):
 
 
 def test_mid_size_with_particles(kg, orc):
-    """nTheta=512 x nPhi=1024, radius 1, dt=0.002, l<=16, 2^20 particles:
-    fields and particles against the FP64 oracle after 3 steps, then 1000
-    steps keep every particle on the sphere and every field finite."""
+    """The mid-size configuration: nTheta=512 x nPhi=1024, radius 1,
+    dt=0.002, l<=16, 2^20 particles advected with RK2.  Fields and particles
+    against the FP64 oracle after 1 and 100 steps (fields: relative L2 <=
+    1e-5; particles: relative L2 of their positions on the sphere <= 1e-5,
+    none more than 1e-4 of the radius away), then the rest of the 1000 steps
+    keep every particle on the sphere and every field finite."""
     npart = 1 << 20
-    st, s, o = make_pair(kg, orc, 512, 0.002, lmax=16, npart=npart)
-    s.step_n(3)
-    o.step(3)
-    got, want = s.fields(), o.fields()
-    for k in FIELDS:
-        err = orc.rel_l2(got[k], want[k])
-        assert err <= TOL, "%s after 3 steps (nt=512, 2^20 particles): rel L2 %.3e" % (k, err)
-    gp, wp = got["particles"].astype(np.float64), o.get_state(4)
-    d = np.abs(gp - wp)
-    d[:, 0] = np.minimum(d[:, 0], 2 * np.pi - d[:, 0])
-    assert np.percentile(d, 99.9) < 1e-4, np.percentile(d, 99.9)
-    s.step_n(997)
+    st, s, o = make_pair(kg, orc, 512, 0.002, lmax=16, npart=npart, flags=kg.F_PARTICLE_RK2)
+    done = 0
+    for steps in (1, 100):
+        s.step_n(steps - done)
+        o.step(steps - done)
+        done = steps
+        got, want = s.fields(), o.fields()
+        for k in FIELDS:
+            err = orc.rel_l2(got[k], want[k])
+            assert err <= TOL, "%s after %d steps (nt=512, 2^20 particles): rel L2 %.3e" % (k, steps, err)
+        wp = o.get_state(4)
+        d = chord(got["particles"], wp)
+        rel = np.sqrt(np.sum(d ** 2) / npart)  # positions are unit vectors
+        assert rel <= TOL and d.max() < 1e-4, (steps, rel, d.max())
+    s.step_n(900)
     f = s.fields()
     s.close()
     for k in FIELDS:
@@ -233,17 +315,21 @@ def test_mid_size_with_particles(kg, orc):
 
 
 @pytest.mark.parametrize("nt", [64, 256])
-def test_fbm_velocity_init_vs_reference_arithmetic(kg, orc, nt):
+def test_fbm_velocity_init_vs_reference_code(kg, orc, nt):
     """kamino_init_fbm (the reference's FBM curl-noise velocity, computed on
-    the device) against the oracle's restatement in the reference's host
-    arithmetic: equal bits except where the device and host double sin differ
-    in the last place and that shifts a float rounding."""
+    the device) against the reference's own initialize_velocity
+    (KaminoInitializer.cu:3-134, compiled unchanged and run on the host; the
+    fixture tests/golden/ref_fbm.npz) and against the oracle's restatement:
+    equal bits except where the device and host double sin differ in the
+    last place and that shifts a float rounding."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_fbm.npz"))
     cfg = kg.default_config(n_theta=nt, radius=1.0, dt=0.005)
     with kg.KaminoSolver(config=cfg) as s:
         s.init_fbm()
         gu, gv = s.get_state(kg.U_PHI), s.get_state(kg.U_THETA)
     wu, wv = orc.ref_init_fbm(nt, 1.0)
-    for got, want in ((gu, wu), (gv, wv)):
+    for got, want in ((gu, g["u_phi_%d" % nt]), (gv, g["u_theta_%d" % nt]), (gu, wu), (gv, wv)):
         assert np.all(np.isfinite(got))
         same = np.mean(got.view(np.uint32) == want.view(np.uint32))
         assert same >= 0.9999, same

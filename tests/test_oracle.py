@@ -208,3 +208,16 @@ def test_oracle_state_generator_matches_the_library(kg, orc, nt, lmax, vortex, n
     for k in ("u_phi", "u_theta", "thickness", "particles"):
         assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), k
     assert a["vortex"] == b["vortex"]
+
+
+@pytest.mark.parametrize("nt", [64, 256])
+def test_fbm_restatement_vs_reference_code(orc, nt):
+    """The oracle's FBM velocity restatement against the reference's own
+    initialize_velocity (KaminoInitializer.cu:3-134 compiled unchanged; the
+    fixture is made by tests/golden/make_fbm_golden.py): bit for bit."""
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_fbm.npz"))
+    wu, wv = orc.ref_init_fbm(nt, 1.0)
+    for got, key in ((wu, "u_phi_%d" % nt), (wv, "u_theta_%d" % nt)):
+        ref = g[key]
+        assert got.shape == ref.shape
+        assert np.array_equal(np.asarray(got, np.float32).view(np.uint32), ref.view(np.uint32)), key
