@@ -69,6 +69,11 @@ __device__ __forceinline__ bool next_item(int* counter, int n, const int2* __res
     return true;
 }
 
+// CELLS: every sphere of the batch has the cell-exact sampler and no
+// particles, so a work item is cell tiles only and the kernel holds none of
+// the reference-rounding or particle code (which would otherwise set its
+// register budget: the general instance spills).
+template <bool CELLS>
 __global__ void __launch_bounds__(kk::ADV_THREADS, 8) kb_advect(const KSphere* __restrict__ sph,
                                                               const int2* __restrict__ items, int n, int* counter,
                                                               int cu, int cr, int tiles_per_item)
@@ -78,6 +83,14 @@ __global__ void __launch_bounds__(kk::ADV_THREADS, 8) kb_advect(const KSphere* _
     int2 w;
     while (next_item(counter, n, items, sph, tiles_per_item, &s, &s_item, &w)) {
         const int t0 = w.y * tiles_per_item, t1 = min(t0 + tiles_per_item, s.nb_adv);
+        if constexpr (CELLS) {
+            // the item's sphere constants and pointers in registers
+            const KGeo g = s.g;
+            const float *u = s.b.u[cu], *v = s.b.v[cu], *rho = s.b.rho[cr], *cc = s.b.cell_c, *cv = s.b.cell_v;
+            float *uo = s.b.u[1 - cu], *vo = s.b.v[1 - cu], *ro = s.b.rho[1 - cr];
+            for (int t = t0; t < t1; t++) kk::advect_cells_tile(g, u, v, rho, uo, vo, ro, cc, cv, t, threadIdx.x);
+            continue;
+        }
         for (int t = t0; t < t1; t++) {
             if (s.ref)
                 kk::advect_tile<true>(s.g, s.b, cu, 1 - cu, cr, 1 - cr, s.nb_u, s.nb_v, s.nb_r, t, threadIdx.x);
@@ -193,6 +206,7 @@ struct Engine {
     int fft_block = 128;  // threads of the FFT kernels: the largest sphere's fft_threads
     int fft_resident = 1; // FFT CTAs of that size resident per SM (registers, shared memory)
     int cls = 1024;       // size class of the FFT and solve kernels: the largest sphere's
+    bool cells_only = true;  // no sphere has particles or the reference-rounding sampler
     Shapes shapes;
     int cu = 0, cr = 0;
     cudaGraphExec_t graph[2][2] = {};
@@ -268,6 +282,8 @@ struct Engine {
         }
         cu = pu;
         cr = pr;
+        cells_only = true;
+        for (const KSphere& s : host_desc) cells_only = cells_only && !s.ref && s.b.npart == 0;
         // work tables, largest sphere first
         std::vector<int> order(hs.size());
         for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
@@ -351,8 +367,8 @@ struct Engine {
     {
         BCUDA(cudaMemsetAsync(d_counters, 0, sizeof(int) * ST_COUNT, stream));
         const int tpi = std::max(1, shapes.adv_tiles_per_item);
-        kb_advect<<<grid(ST_ADV), kk::ADV_THREADS, 0, stream>>>(d_desc, d_items + item_off[ST_ADV],
-                                                                 n_items[ST_ADV], d_counters + ST_ADV, c, r, tpi);
+        (cells_only ? kb_advect<true> : kb_advect<false>)<<<grid(ST_ADV), kk::ADV_THREADS, 0, stream>>>(
+            d_desc, d_items + item_off[ST_ADV], n_items[ST_ADV], d_counters + ST_ADV, c, r, tpi);
         kb_geo<<<grid(ST_GEO), kk::ELEM_THREADS, 0, stream>>>(d_desc, d_items + item_off[ST_GEO], n_items[ST_GEO],
                                                                d_counters + ST_GEO, 1 - c, tpi);
         div_stage(cls)<<<grid(ST_DIV), fft_block, smem_fft, stream>>>(d_desc, d_items + item_off[ST_DIV],

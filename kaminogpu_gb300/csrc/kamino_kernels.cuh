@@ -136,6 +136,25 @@ inline void adv_tiles(const KGeo& g, int& nb_u, int& nb_v, int& nb_r)
     }
 }
 
+// Cell tile `blk` of the cell-exact advection (one cell per thread, its three
+// quantities): the whole tile when the sphere has no particles and the
+// cell-exact sampler, as the batched kernel for such spheres runs it.
+__device__ __forceinline__ void advect_cells_tile(const KGeo& g, const float* __restrict__ u,
+                                                  const float* __restrict__ v, const float* __restrict__ rho,
+                                                  float* __restrict__ uo, float* __restrict__ vo,
+                                                  float* __restrict__ ro, const float* __restrict__ cell_c,
+                                                  const float* __restrict__ cell_v, int blk, int tid)
+{
+    const int idx = blk * ADV_THREADS + tid;
+    if (idx >= g.nt * g.np) return;
+    const int j = idx >> (g.log2nt + 1), i = idx & g.mask;
+    float ou, ov = 0.0f, orr;
+    advect_cell3(u, v, rho, i, j, __ldg(cell_c + j), __ldg(cell_v + j), g.cellTheta, g, ou, ov, orr);
+    uo[idx] = ou;
+    if (j < g.nt - 1) vo[idx] = ov;
+    ro[idx] = orr;
+}
+
 // Tile `blk` of the advection, thread `tid`; REF selects the
 // reference-rounding (radian) sampler, otherwise the cell-exact one.
 template <bool REF>
@@ -146,14 +165,7 @@ __device__ __forceinline__ void advect_tile(const KGeo& g, const KBufs& b, int s
     const float* __restrict__ v = b.v[suv];
     const int lg = g.log2nt + 1;  // log2(nPhi)
     if (!REF && blk < nb_u) {
-        const int idx = blk * ADV_THREADS + tid;
-        if (idx >= g.nt * g.np) return;
-        const int j = idx >> lg, i = idx & g.mask;
-        float ou, ov = 0.0f, orr;
-        advect_cell3(u, v, b.rho[sr], i, j, __ldg(b.cell_c + j), __ldg(b.cell_v + j), g.cellTheta, g, ou, ov, orr);
-        b.u[duv][idx] = ou;
-        if (j < g.nt - 1) b.v[duv][idx] = ov;
-        b.rho[dr][idx] = orr;
+        advect_cells_tile(g, u, v, b.rho[sr], b.u[duv], b.v[duv], b.rho[dr], b.cell_c, b.cell_v, blk, tid);
         return;
     }
     if (REF && blk < nb_u + nb_v + nb_r) {
