@@ -390,6 +390,13 @@ struct Engine {
     {
         if (hs.empty() || n <= 0) return KAMINO_OK;
         BCUDA(cudaSetDevice(device));
+        // the particles' visiting orders that are due, on the spheres' own
+        // streams, before the batch's launches
+        for (kamino_handle h : hs) {
+            int launched = 0;
+            if (int rc = kamino_internal_sort_particles(h, &launched)) return rc;
+            if (launched) BCUDA(cudaStreamSynchronize(kamino_internal_stream(h)));
+        }
         for (int k = 0; k < n; k++) {
             cudaGraphExec_t& ge = graph[cu][cr];
             if (!ge) {

@@ -37,6 +37,10 @@ int kamino_internal_set_counters(kamino_handle h, int cur_uv, int cur_r, int64_t
 // Re-targets a handle of the same nTheta to a new radius / dt / flags and
 // zeroes its state, so pooled device memory can serve a new request.
 int kamino_internal_reset(kamino_handle h, const kamino_config* cfg);
+// Rebuilds the particles' visiting order (KBufs::pperm) on the handle's
+// stream when it is due (*launched: whether it did); the batched engine
+// calls it before its steps.
+int kamino_internal_sort_particles(kamino_handle h, int* launched);
 // The handle's own stream (its steps and copies are ordered on it).
 cudaStream_t kamino_internal_stream(kamino_handle h);
 // The handle's configuration as created.
@@ -108,4 +112,10 @@ struct KBufs {
     float2* tw;      // e^{-2 pi i k / nt}, k < nt/2
     float2* rt;      // e^{-i pi m / nt},  m <= nt
     int64_t npart;
+    // Order in which the advection visits the particles: a permutation of
+    // 0 .. npart-1, rebuilt every few steps so that consecutive threads take
+    // particles of the same block of cells (their gathers then share cache
+    // lines).  Each particle's update does not depend on the order.  Null:
+    // index order.
+    const int* pperm;
 };

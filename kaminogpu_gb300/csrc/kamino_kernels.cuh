@@ -192,6 +192,7 @@ __device__ __forceinline__ void advect_tile(const KGeo& g, const KBufs& b, int s
     blk -= nb_u + nb_v + nb_r;
     int64_t k = (int64_t)blk * ADV_THREADS + tid;
     if (k >= b.npart) return;
+    if (b.pperm) k = __ldg(b.pperm + k);  // the particle this thread takes
     float2 out;
     advect_particle(g, u, v, b.part[sr][k], out);
     b.part[dr][k] = out;
@@ -235,8 +236,9 @@ __global__ void __launch_bounds__(ADV_THREADS, 8) k_advect_part(KGeo g, KBufs b,
         return;
     }
     if constexpr ((MASK & 1) != 0) {
-        const int64_t k = (int64_t)(blk - nb_u) * ADV_THREADS + tid;
+        int64_t k = (int64_t)(blk - nb_u) * ADV_THREADS + tid;
         if (k >= b.npart) return;
+        if (b.pperm) k = __ldg(b.pperm + k);
         float2 out;
         advect_particle(g, u, v, b.part[sr][k], out);
         b.part[dr][k] = out;
@@ -1871,6 +1873,83 @@ inline cudaError_t flush_l2(void* buf, size_t bytes, int pattern, cudaStream_t s
     if (e != cudaSuccess) return e;
     k_flush_read<<<1216, 256, 0, s>>>(reinterpret_cast<const float4*>(buf), bytes / 16, static_cast<float*>(buf));
     return cudaGetLastError();
+}
+
+// ------------------------------------------------ particle visiting order
+// A counting sort of the particles by the block of 4 rows x 32 columns of
+// cells they sit in: k_pkeys keys each particle and counts the blocks,
+// k_pscan turns the counts into offsets, k_pscatter lists the particles by
+// block.  Within a block the order is whatever the atomics give; the
+// result is a permutation either way.
+constexpr int PBLK_ROWS_LOG2 = 2, PBLK_COLS_LOG2 = 5;
+__host__ __device__ inline int pblocks(int nt)
+{
+    return (nt >> PBLK_ROWS_LOG2) * ((2 * nt) >> PBLK_COLS_LOG2);
+}
+
+__global__ void __launch_bounds__(ELEM_THREADS) k_pkeys(KGeo g, const float2* __restrict__ part, int64_t n,
+                                                        int* __restrict__ keys, int* __restrict__ counts)
+{
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float2 p = __ldg(part + k);
+    // cell of (phi, theta), clamped: any position (even a non-finite one)
+    // gets a valid block
+    const float fr = p.y * g.invh, fc = p.x * g.invh;
+    const int r = fr >= 0.0f ? (fr < (float)(g.nt - 1) ? (int)fr : g.nt - 1) : 0;
+    const int c = fc >= 0.0f ? (fc < (float)g.mask ? (int)fc : g.mask) : 0;
+    const int key = (r >> PBLK_ROWS_LOG2) * (g.np >> PBLK_COLS_LOG2) + (c >> PBLK_COLS_LOG2);
+    keys[k] = key;
+    atomicAdd(counts + key, 1);
+}
+
+// Exclusive prefix sum of counts[0 .. nb) in place, one CTA of 1024 threads.
+__global__ void __launch_bounds__(1024) k_pscan(int* __restrict__ counts, int nb)
+{
+    __shared__ int wsum[32];
+    const int t = threadIdx.x, per = (nb + 1023) / 1024, b0 = t * per, b1 = min(b0 + per, nb);
+    int local = 0;
+    for (int i = b0; i < b1; i++) local += counts[i];
+    // inclusive scan of the 1024 partial sums: within warps, then of the warp totals
+    int x = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if ((t & 31) >= o) x += y;
+    }
+    if ((t & 31) == 31) wsum[t >> 5] = x;
+    __syncthreads();
+    if (t < 32) {
+        int w = wsum[t];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (t >= o) w += y;
+        }
+        wsum[t] = w;
+    }
+    __syncthreads();
+    int run = x - local + ((t >> 5) ? wsum[(t >> 5) - 1] : 0);  // exclusive prefix of this thread's range
+    for (int i = b0; i < b1; i++) {
+        const int c = counts[i];
+        counts[i] = run;
+        run += c;
+    }
+}
+
+// The index order, 0 .. n-1: the visiting order before any sort.
+__global__ void __launch_bounds__(ELEM_THREADS) k_piota(int* __restrict__ perm, int64_t n)
+{
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) perm[k] = (int)k;
+}
+
+__global__ void __launch_bounds__(ELEM_THREADS) k_pscatter(const int* __restrict__ keys, int64_t n,
+                                                           int* __restrict__ offsets, int* __restrict__ perm)
+{
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    perm[atomicAdd(offsets + keys[k], 1)] = (int)k;
 }
 
 // ------------------------------------------------------------- probes

@@ -64,7 +64,17 @@ struct kamino_solver_s {
     cudaEvent_t ev_rho = nullptr;      // kamino_step_host: the thickness is on the device
     cudaEvent_t ev_u = nullptr;        // kamino_step_host: u_phi of the step is final
     KFrames* frames = nullptr;         // frame output (kamino_frames.cu), made on first use
+    // the particles' visiting order (KBufs::pperm): rebuilt by sort_particles
+    // every kSortEvery steps, and before the first step after the particles
+    // were set from outside
+    int* pkeys = nullptr;
+    int* pcounts = nullptr;
+    int64_t sorted_at = -1;  // step count of the last sort; -1: due
 };
+
+// Steps between rebuilds of the particles' visiting order: particles move
+// about a cell a step, so the order stays mostly block by block for a few.
+static const int kSortEvery = 8;
 
 static const char* const kKernelNames[] = {"k_advect", "k_geo_centers", "k_div_fft",
                                            "k_solve",  "k_ifft_u",      "k_vgrad"};
@@ -297,7 +307,9 @@ extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
     const size_t rowf = align_up(sizeof(float) * nt), rowd = align_up(sizeof(double) * nt);
     const size_t tw = align_up(sizeof(float2) * nt), rt = align_up(sizeof(float2) * (nt + 1));
     const size_t s64 = align_up(sizeof(double) * kk::s64_stride(nt) * std::max(h->nfp64, 1));
-    size_t total = 9 * field + 2 * spec + 2 * part + 13 * rowf + 4 * rowd + tw + rt + s64;
+    const size_t pint = npart > 0 ? align_up(sizeof(int) * (size_t)npart) : 0;  // visiting order, sort keys
+    const size_t pcnt = npart > 0 ? align_up(sizeof(int) * (size_t)kk::pblocks(nt)) : 0;
+    size_t total = 9 * field + 2 * spec + 2 * part + 13 * rowf + 4 * rowd + tw + rt + s64 + 2 * pint + pcnt;
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&h->arena, total);
     if (e != cudaSuccess) {
@@ -345,6 +357,13 @@ extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
     b.tw = (float2*)take(tw);
     b.rt = (float2*)take(rt);
     b.npart = npart;
+    if (npart > 0) {
+        b.pperm = (const int*)take(pint);
+        h->pkeys = (int*)take(pint);
+        h->pcounts = (int*)take(pcnt);
+    } else {
+        b.pperm = nullptr;
+    }
 
     rc = KAMINO_OK;
     do {
@@ -392,6 +411,8 @@ extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
         }
         if (e != cudaSuccess) break;
         kk::k_tables<<<(nt + 127) / 128, 128, 0, h->stream>>>(h->g, h->b);
+        if (npart > 0)  // a valid visiting order from the start (rebuilt before the first step)
+            kk::k_piota<<<(unsigned)((npart + 255) / 256), 256, 0, h->stream>>>(const_cast<int*>(b.pperm), npart);
         e = cudaGetLastError();
         if (e != cudaSuccess) break;
         e = cudaStreamSynchronize(h->stream);  // host vectors above go out of scope
@@ -589,6 +610,24 @@ static int check_handle(kamino_solver_s* h)
     return KAMINO_OK;
 }
 
+// Rebuilds the particles' visiting order from their current positions (a
+// counting sort by block of cells, on the handle's stream) when it is due.
+static int sort_particles(kamino_solver_s* h)
+{
+    const int64_t n = h->b.npart;
+    if (n == 0 || (h->sorted_at >= 0 && h->steps - h->sorted_at < kSortEvery)) return KAMINO_OK;
+    const KGeo& g = h->g;
+    const int nb = kk::pblocks(g.nt), T = kk::ELEM_THREADS;
+    const unsigned blocks = (unsigned)((n + T - 1) / T);
+    KCUDA(cudaMemsetAsync(h->pcounts, 0, sizeof(int) * (size_t)nb, h->stream));
+    kk::k_pkeys<<<blocks, T, 0, h->stream>>>(g, h->b.part[h->cur_r], n, h->pkeys, h->pcounts);
+    kk::k_pscan<<<1, 1024, 0, h->stream>>>(h->pcounts, nb);
+    kk::k_pscatter<<<blocks, T, 0, h->stream>>>(h->pkeys, n, h->pcounts, const_cast<int*>(h->b.pperm));
+    KCUDA(cudaGetLastError());
+    h->sorted_at = h->steps;
+    return KAMINO_OK;
+}
+
 // Rebuild dt-dependent tables when KAMINO_F_HONOR_STEP_DT asks for a new dt:
 // every table and constant kamino_create derives from the configured dt, so
 // the step equals that of a handle created with this dt.
@@ -621,6 +660,7 @@ extern "C" int kamino_step(kamino_handle h, float dt)
     if (rc) return rc;
     h->last_dt = dt;  // stored, as stepForward does (KaminoSolver.cu:199)
     rc = apply_dt(h, dt);
+    if (!rc) rc = sort_particles(h);
     if (rc) return rc;
     cudaGraphExec_t ge = nullptr;
     rc = get_graph(h, 1, &ge);
@@ -640,6 +680,7 @@ extern "C" int kamino_step_n(kamino_handle h, int n)
     if (n < 0) return kamino_fail(KAMINO_ERR_INVALID, "step count %d < 0", n);
     for (int k = 0; k < n;) {
         int s = (n - k >= 2) ? 2 : 1;
+        if ((rc = sort_particles(h))) return rc;
         cudaGraphExec_t ge = nullptr;
         rc = get_graph(h, s, &ge);
         if (rc) return rc;
@@ -659,7 +700,8 @@ extern "C" int kamino_advection(kamino_handle h)
 {
     int rc = check_handle(h);
     if (rc) return rc;
-    rc = launch_advect(h, h->cur_uv, 1 - h->cur_uv, h->cur_r, 1 - h->cur_r);
+    rc = sort_particles(h);
+    if (!rc) rc = launch_advect(h, h->cur_uv, 1 - h->cur_uv, h->cur_r, 1 - h->cur_r);
     if (rc) return rc;
     h->cur_uv ^= 1;
     h->cur_r ^= 1;
@@ -746,11 +788,22 @@ int kamino_internal_get_counters(kamino_handle h, int* cur_uv, int* cur_r, int64
     return KAMINO_OK;
 }
 
+int kamino_internal_sort_particles(kamino_handle h, int* launched)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    const int64_t before = h->sorted_at;
+    rc = sort_particles(h);
+    if (launched) *launched = h->sorted_at != before;
+    return rc;
+}
+
 int kamino_internal_set_counters(kamino_handle h, int cur_uv, int cur_r, int64_t steps, double time)
 {
     if (!h) return kamino_fail(KAMINO_ERR_INVALID, "null handle");
     h->cur_uv = cur_uv & 1;
     h->cur_r = cur_r & 1;
+    if (steps != h->steps) h->sorted_at = -1;
     h->steps = steps;
     h->time = time;
     return KAMINO_OK;
@@ -790,6 +843,7 @@ int kamino_internal_reset(kamino_handle h, const kamino_config* cfg)
     h->steps = 0;
     h->time = 0.0;
     h->last_dt = g.dt;
+    h->sorted_at = -1;
     destroy_graphs(h);
     const int nt = g.nt;
     std::vector<float> cellc(nt), cellv(nt);
@@ -876,6 +930,7 @@ static int copy_field(kamino_solver_s* h, int field, void* other, size_t pitch, 
     rc = field_geometry(h, field, &rows);
     if (rc) return rc;
     float* d = field_dev(h, field);
+    if (field == KAMINO_PARTICLES && to_device) h->sorted_at = -1;  // the visiting order is rebuilt before the next step
     if (field == KAMINO_PARTICLES) {
         size_t n = sizeof(float2) * (size_t)h->b.npart;
         if (n == 0) return KAMINO_OK;
@@ -938,7 +993,7 @@ extern "C" int kamino_step_host(kamino_handle h, float dt, const float* u_phi_in
             KCUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     }
     h->last_dt = dt;
-    if ((rc = apply_dt(h, dt))) return rc;
+    if ((rc = apply_dt(h, dt)) || (rc = sort_particles(h))) return rc;
     const int rows = h->g.nt;
     auto d2h = [&](float* dst, const float* src, int nrows) {
         if (pitch_bytes == w) return cudaMemcpyAsync(dst, src, w * nrows, cudaMemcpyDeviceToHost, h->io_stream);
@@ -1081,6 +1136,7 @@ extern "C" int kamino_time_kernels(kamino_handle h, int reps, int flush_l2, doub
     cudaEvent_t ev[2][kNumKernels + 1];
     for (auto& row : ev)
         for (auto& e : row) KCUDA(cudaEventCreate(&e));
+    if ((rc = sort_particles(h))) return rc;
     // one graph per parity, each with event nodes around every kernel
     cudaGraphExec_t ge[2][2] = {};
     for (int r = 0; r < reps && rc == KAMINO_OK; r++) {

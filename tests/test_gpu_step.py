@@ -375,3 +375,28 @@ def test_pole_sign_flip_vs_fp64_oracle(kg, orc, nt, steps):
         err = orc.rel_l2(got[k], want[k])
         assert err <= TOL, "%s after %d steps with the pole sign flip: rel L2 %.3e" % (k, steps, err)
     assert np.abs(got["particles"].astype(np.float64) - o.get_state(4)).max() < 1e-4
+
+
+@pytest.mark.parametrize("flags", [0, 1])
+def test_particle_visiting_order_does_not_change_results(kg, orc, flags):
+    """The advection visits the particles block by block of cells, in an
+    order rebuilt every few steps from their positions; each particle's update
+    is independent of the order, so stepping with the order rebuilt before
+    every step (the particles set again from outside each time) gives the same
+    bits as the default schedule, and as the index order the order starts
+    from."""
+    nt, npart = 128, 200000
+    st = kg.make_initial_state(nt, lmax=8, seed=17, n_particles=npart)
+    cfg = kg.default_config(n_theta=nt, radius=1.0, dt=0.004, n_particles=npart, flags=flags)
+    with kg.KaminoSolver(config=cfg) as a, kg.KaminoSolver(config=cfg) as b:
+        a.load(st)
+        b.load(st)
+        a.step_n(20)
+        for _ in range(20):
+            b.set_state(kg.PARTICLES, b.get_state(kg.PARTICLES))
+            b.stepForward()
+        pa, pb = a.get_state(kg.PARTICLES), b.get_state(kg.PARTICLES)
+        fa, fb = a.fields(), b.fields()
+    assert np.array_equal(pa.view(np.uint32), pb.view(np.uint32))
+    for k in FIELDS:
+        assert np.array_equal(fa[k].view(np.uint32), fb[k].view(np.uint32)), k
