@@ -257,16 +257,14 @@ __device__ __forceinline__ float f4get(const float4& a, int k)
     return k == 0 ? a.x : (k == 1 ? a.y : (k == 2 ? a.z : a.w));
 }
 
-// geometricFillKernel (KaminoCore.cu:457-514) for cells 4q .. 4q+3: u, v
-// averaged to the cell centre, the metric-term root, u' and v' at centres.
-__device__ __forceinline__ void geo_tile(const KGeo& g, const KBufs& b, int src, int q)
+// geometricFillKernel (KaminoCore.cu:457-514) for the cells i .. i+3 of row
+// j (i a multiple of 4): u, v averaged to the cell centre, the metric-term
+// root, u' and v' at the centres.
+__device__ __forceinline__ void geo_group(const KGeo& g, const float* __restrict__ u, const float* __restrict__ v,
+                                          const float* __restrict__ gfac, int j, int i, float (&cu)[4],
+                                          float (&cv)[4])
 {
-    const int idx = q * ELEM_VEC;
-    if (idx >= g.nt * g.np) return;
-    const int lg = g.log2nt + 1;
-    const int j = idx >> lg, i = idx & g.mask;
-    const float* __restrict__ u = b.u[src];
-    const float* __restrict__ v = b.v[src];
+    const int idx = (j << (g.log2nt + 1)) + i;
     const float4 uc = ldg4(u + idx);
     const float un = __ldg(u + (idx & ~g.mask) + ((i + ELEM_VEC) & g.mask));
     float vp[ELEM_VEC];
@@ -281,13 +279,24 @@ __device__ __forceinline__ void geo_tile(const KGeo& g, const KBufs& b, int src,
         for (int k = 0; k < ELEM_VEC; k++) vp[k] = 0.5f * __fadd_rn(f4get(a, k), f4get(c, k));
     }
     const float uu[ELEM_VEC + 1] = {uc.x, uc.y, uc.z, uc.w, un};
-    const float G = __ldg(b.gfac + j);
-    float up[ELEM_VEC], cu[ELEM_VEC], cv[ELEM_VEC];
+    const float G = __ldg(gfac + j);
+    float up[ELEM_VEC];
 #pragma unroll
     for (int k = 0; k < ELEM_VEC; k++) up[k] = 0.5f * __fadd_rn(uu[k], uu[k + 1]);
     geo_roots<ELEM_VEC>(G, up, vp, cu);
 #pragma unroll
     for (int k = 0; k < ELEM_VEC; k++) cv[k] = __fadd_rn(vp[k], __fmul_rn(__fmul_rn(G, cu[k]), cu[k]));
+}
+
+// The geometric step for cells 4q .. 4q+3 of the field: the centre values
+// into the scratch cu, cv.
+__device__ __forceinline__ void geo_tile(const KGeo& g, const KBufs& b, int src, int q)
+{
+    const int idx = q * ELEM_VEC;
+    if (idx >= g.nt * g.np) return;
+    const int j = idx >> (g.log2nt + 1), i = idx & g.mask;
+    float cu[ELEM_VEC], cv[ELEM_VEC];
+    geo_group(g, b.u[src], b.v[src], b.gfac, j, i, cu, cv);
     *reinterpret_cast<float4*>(b.cu + idx) = make_float4(cu[0], cu[1], cu[2], cu[3]);
     *reinterpret_cast<float4*>(b.cv + idx) = make_float4(cv[0], cv[1], cv[2], cv[3]);
 }
