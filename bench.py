@@ -270,6 +270,7 @@ def run_ours(args, ws, rank, local, dist):
         "dominant_kernel": dom,
         "clocks": ck.summary(),
     }
+    out["fp64_modes_0"] = bench_fp64_modes_0(kg, local, st, steps=min(args.steps, 500))
     if not args.no_config2:
         out["config2"] = bench_particles(kg, local, hbm)
     if not args.no_batched:
@@ -281,6 +282,23 @@ def run_ours(args, ws, rank, local, dist):
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(st, seconds=10.0)
     return out
+
+
+def bench_fp64_modes_0(kg, local, st, steps):
+    """The same sphere with every Fourier mode solved in FP32 (the dominance
+    form), beside the precision form's FP64 for |m| <= 4."""
+    cfg = kg.default_config(n_theta=NT, radius=1.0, dt=DT, fp64_modes=0, device=local)
+    with kg.KaminoSolver(config=cfg) as s:
+        s.load(st)
+        s.step_n(5)
+        s.synchronize()
+        kms = s.time_kernels(reps=10, flush_l2=True)
+        s.load(st)
+        s.step_n(3)
+        s.synchronize()
+        ms = s.time_steps(steps, flush_l2=True) / steps
+    return {"ms_per_step": ms, "cell_steps_per_s": NT * 2 * NT / (ms / 1e3), "k_solve_ms": kms["k_solve"],
+            "what": "fp64_modes=0: every mode solved in FP32, %d timed steps" % steps}
 
 
 def bench_particles(kg, local, hbm, npart=1 << 20, steps=200):
@@ -520,12 +538,15 @@ def bench_served(kg, local, seconds, rate=200.0, budget=120 << 30):
     with Clocks(local) as ck:
         t0 = time.perf_counter()
         rids = [srv.submit(cfg(nt), state(nt, i), st) for i, (nt, st) in enumerate(reqs)]
+        t_submit = time.perf_counter() - t0
         done = 0
         while done < len(reqs):
             done += srv.poll()
         wall_srv = time.perf_counter() - t0
     stats = srv.stats()
+    t0 = time.perf_counter()
     served_res = {i: srv.fetch(rids[i]) for i in range(0, len(reqs), 13)}
+    t_fetch = (time.perf_counter() - t0) / max(1, len(served_res))
     srv.close()
     handles = {}
     for nt in sorted({nt for nt, _ in reqs}):
@@ -550,7 +571,20 @@ def bench_served(kg, local, seconds, rate=200.0, budget=120 << 30):
                           "p99_latency_s": stats["p99_latency_s"],
                           "plain_per_request": {"value": cs_total / wall_plain, "wall_s": wall_plain},
                           "speedup_vs_plain": wall_plain / wall_srv, "bitwise_equal_to_plain": bitwise,
-                          "requests_compared": len(served_res), "clocks": ck.summary()}
+                          "requests_compared": len(served_res), "clocks": ck.summary(),
+                          "breakdown": {
+                              "wall_s": wall_srv,
+                              "host_submit_s": t_submit,
+                              "host_poll_s": stats["poll_seconds"],
+                              "host_fetch_s_per_request": t_fetch,
+                              "batched_rounds": stats["batched_rounds"],
+                              "batched_round_device_s": stats["batched_round_seconds"],
+                              "solo_device_s_summed": stats["solo_seconds"],
+                              "solo_cell_steps": stats["solo_cell_steps"],
+                              "batched_cell_steps": stats["batched_cell_steps"],
+                              "what": "batched rounds run one at a time on the engine's stream; one-sphere "
+                                      "runs (nTheta >= 512) on their own streams, up to 3 at once, so their "
+                                      "device times overlap each other and the rounds"}}
     # open loop: Poisson arrivals
     rng = np.random.default_rng(6)
     n_open = int(rate * seconds)

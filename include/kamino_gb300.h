@@ -420,6 +420,14 @@ typedef struct kamino_server_stats {
     double busy_seconds;      /* wall time with at least one resident sphere */
     double p50_latency_s, p99_latency_s, mean_latency_s;
     size_t resident_bytes, peak_resident_bytes;
+    /* where the time and the work went */
+    int64_t solo_cell_steps;       /* cell-steps of spheres run as one-sphere graphs */
+    int64_t batched_cell_steps;    /* cell-steps of the batched rounds            */
+    int64_t batched_rounds;        /* batched rounds completed                    */
+    double batched_round_seconds;  /* device time of those rounds (CUDA events)   */
+    double solo_seconds;           /* device time of the one-sphere runs, summed
+                                      (they can overlap each other)              */
+    double poll_seconds;           /* host wall time inside kamino_server_poll    */
 } kamino_server_stats;
 
 int kamino_server_create(const kamino_server_config* cfg, kamino_server* out);

@@ -92,6 +92,12 @@ class KaminoServerStats(ctypes.Structure):
         ("mean_latency_s", ctypes.c_double),
         ("resident_bytes", ctypes.c_size_t),
         ("peak_resident_bytes", ctypes.c_size_t),
+        ("solo_cell_steps", ctypes.c_int64),
+        ("batched_cell_steps", ctypes.c_int64),
+        ("batched_rounds", ctypes.c_int64),
+        ("batched_round_seconds", ctypes.c_double),
+        ("solo_seconds", ctypes.c_double),
+        ("poll_seconds", ctypes.c_double),
     ]
 
 

@@ -674,6 +674,7 @@ struct Request {
     int status = KAMINO_OK;  // KAMINO_ERR_BUDGET for a request that can never fit
     bool solo = false;       // advanced by its own one-sphere graphs
     cudaEvent_t finished = nullptr;  // solo: recorded after its last step
+    cudaEvent_t started = nullptr;   // solo: recorded before its first step
 };
 
 } // namespace
@@ -690,6 +691,9 @@ struct kamino_server_s {
     std::map<int, size_t> bytes_for;                 // device bytes of a handle by n_theta
     std::vector<double> latencies;
     int64_t cell_steps = 0, completed = 0;
+    int64_t solo_cells = 0, batched_cells = 0, rounds = 0;
+    double round_seconds = 0, solo_seconds = 0, poll_seconds = 0;
+    cudaEvent_t round_start = nullptr;
     size_t resident_bytes = 0, peak_bytes = 0;
     size_t pooled_bytes = 0;  // free handles kept for reuse also hold HBM
     double busy = 0;
@@ -711,6 +715,7 @@ struct kamino_server_s {
             for (kamino_handle h : kv.second) kamino_destroy(h);
         for (cudaEvent_t e : free_events) cudaEventDestroy(e);
         if (round_done) cudaEventDestroy(round_done);
+        if (round_start) cudaEventDestroy(round_start);
     }
     int solo_n_theta() const { return cfg.solo_n_theta > 0 ? cfg.solo_n_theta : 512; }
     int solo_slots() const { return cfg.solo_slots > 0 ? cfg.solo_slots : 3; }
@@ -735,7 +740,7 @@ extern "C" int kamino_server_create(const kamino_server_config* cfg, kamino_serv
     if (s->cfg.steps_per_round <= 0) s->cfg.steps_per_round = 10;
     s->t0 = std::chrono::steady_clock::now();
     int rc = s->eng.init(cfg->device);
-    if (!rc && cudaEventCreateWithFlags(&s->round_done, cudaEventDisableTiming) != cudaSuccess)
+    if (!rc && (cudaEventCreate(&s->round_done) != cudaSuccess || cudaEventCreate(&s->round_start) != cudaSuccess))
         rc = kamino_fail(KAMINO_ERR_CUDA, "kamino_server_create: event");
     if (rc) {
         delete s;
@@ -841,6 +846,14 @@ static int server_retire(kamino_server s, const std::shared_ptr<Request>& r, dou
     s->pooled_bytes += r->bytes;
     s->pool[pool_key(r->cfg)].push_back(r->h);
     r->h = nullptr;
+    if (r->started && r->finished) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, r->started, r->finished) == cudaSuccess) s->solo_seconds += ms / 1e3;
+    }
+    if (r->started) {
+        cudaEventDestroy(r->started);
+        r->started = nullptr;
+    }
     if (r->finished) {
         s->free_events.push_back(r->finished);
         r->finished = nullptr;
@@ -857,9 +870,19 @@ static int server_retire(kamino_server s, const std::shared_ptr<Request>& r, dou
 //     joins the next round;
 //  3. if no round is in flight, the batched spheres take a round of
 //     min(steps_per_round, fewest steps left) steps.
+static int server_poll(kamino_server s, int* n_completed);
+
 extern "C" int kamino_server_poll(kamino_server s, int* n_completed)
 {
     if (!s) return kamino_fail(KAMINO_ERR_INVALID, "null server");
+    const double t_in = s->now();
+    const int rc = server_poll(s, n_completed);
+    s->poll_seconds += s->now() - t_in;
+    return rc;
+}
+
+static int server_poll(kamino_server s, int* n_completed)
+{
     Engine& e = s->eng;
     BCUDA(cudaSetDevice(e.device));
     const double t = s->now();
@@ -870,6 +893,9 @@ extern "C" int kamino_server_poll(kamino_server s, int* n_completed)
         cudaError_t q = cudaEventQuery(s->round_done);
         if (q == cudaSuccess) {
             s->round_pending = false;
+            float ms = 0;
+            if (cudaEventElapsedTime(&ms, s->round_start, s->round_done) == cudaSuccess) s->round_seconds += ms / 1e3;
+            s->rounds++;
         } else if (q != cudaErrorNotReady) {
             return kamino_fail(KAMINO_ERR_CUDA, "batched round: %s", cudaGetErrorString(q));
         }
@@ -943,23 +969,29 @@ extern "C" int kamino_server_poll(kamino_server s, int* n_completed)
             if (!s->free_events.empty()) {
                 r->finished = s->free_events.back();
                 s->free_events.pop_back();
-            } else if (cudaEventCreateWithFlags(&r->finished, cudaEventDisableTiming) != cudaSuccess) {
+            } else if (cudaEventCreate(&r->finished) != cudaSuccess) {
                 rc = kamino_fail(KAMINO_ERR_CUDA, "request event");
             }
+            if (!rc && (cudaEventCreate(&r->started) != cudaSuccess ||
+                        cudaEventRecord(r->started, kamino_internal_stream(h)) != cudaSuccess))
+                rc = kamino_fail(KAMINO_ERR_CUDA, "request start event");
             if (!rc) rc = kamino_step_n(h, r->remaining);
             if (!rc && cudaEventRecord(r->finished, kamino_internal_stream(h)) != cudaSuccess)
                 rc = kamino_fail(KAMINO_ERR_CUDA, "request event record");
             if (!rc) {
-                s->cell_steps += (int64_t)r->remaining * r->cfg.n_theta * 2 * r->cfg.n_theta;
+                const int64_t cs = (int64_t)r->remaining * r->cfg.n_theta * 2 * r->cfg.n_theta;
+                s->cell_steps += cs;
+                s->solo_cells += cs;
                 r->remaining = 0;
             }
         }
         if (rc) {
             if (h) kamino_destroy(h);
-            if (r->finished) {
-                cudaEventDestroy(r->finished);
-                r->finished = nullptr;
-            }
+            for (cudaEvent_t* ev : {&r->finished, &r->started})
+                if (*ev) {
+                    cudaEventDestroy(*ev);
+                    *ev = nullptr;
+                }
             return rc;
         }
         r->h = h;
@@ -990,6 +1022,7 @@ extern "C" int kamino_server_poll(kamino_server s, int* n_completed)
                 if (rc) return rc;
                 s->dirty = false;
             }
+            BCUDA(cudaEventRecord(s->round_start, e.stream));
             int rc = e.step_n(steps);
             if (rc) return rc;
             BCUDA(cudaEventRecord(s->round_done, e.stream));
@@ -997,6 +1030,7 @@ extern "C" int kamino_server_poll(kamino_server s, int* n_completed)
             for (auto& r : s->resident)
                 if (!r->solo) r->remaining -= steps;
             s->cell_steps += (int64_t)steps * e.cells;
+            s->batched_cells += (int64_t)steps * e.cells;
         }
     }
     if (n_completed) *n_completed = done_now;
@@ -1040,6 +1074,12 @@ extern "C" int kamino_server_get_stats(kamino_server s, kamino_server_stats* st)
     st->queued = (int64_t)s->queue.size();
     st->cell_steps = s->cell_steps;
     st->busy_seconds = s->busy;
+    st->solo_cell_steps = s->solo_cells;
+    st->batched_cell_steps = s->batched_cells;
+    st->batched_rounds = s->rounds;
+    st->batched_round_seconds = s->round_seconds;
+    st->solo_seconds = s->solo_seconds;
+    st->poll_seconds = s->poll_seconds;
     std::vector<double> l = s->latencies;
     if (!l.empty()) {
         std::sort(l.begin(), l.end());

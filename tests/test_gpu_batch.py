@@ -83,6 +83,12 @@ def test_server_results_same_alone_and_in_the_mix(kg, orc):
             assert np.array_equal(got[k].view(np.uint32), want[k].view(np.uint32)), (rid, k)
     st = srv.stats()
     assert st["completed"] == len(plan) and st["p99_latency_s"] >= st["p50_latency_s"] > 0
+    # the breakdown: the nTheta=512 request ran alone, the rest in batched rounds
+    cells = sum(nt * 2 * nt * steps for nt, _, steps in plan)
+    solo_cells = sum(nt * 2 * nt * steps for nt, _, steps in plan if nt >= 512)
+    assert st["cell_steps"] == cells and st["solo_cell_steps"] == solo_cells
+    assert st["batched_cell_steps"] == cells - solo_cells and st["batched_rounds"] > 0
+    assert st["batched_round_seconds"] > 0 and st["solo_seconds"] > 0 and st["poll_seconds"] > 0
     srv.close()
 
 
