@@ -220,12 +220,21 @@ __device__ __forceinline__ float sample_cell(const float* __restrict__ f, int i,
     return (vec_flip && s.flipped) ? -r : r;
 }
 
+// Packed pairs (f32x2: one instruction for two FP32 lanes of a register
+// pair, sm_100 and later) carry the two coordinates of a position and the
+// two row lerps of a bilinear sample.  Each lane rounds as the scalar
+// instruction would.
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
 // RK2 back-trace in cells.  (cgp, cgt) is the grid point's staggering
 // offset in cells (u_phi: -1/2, 1/2; u_theta: 0, 1; centred: 0, 1/2); the
 // samplers' own offsets are u_phi (-1/2, 1/2), u_theta (0, 1), centred
 // (0, 1/2), so each sample position is (i, j) + (cg - so) - d exactly.
 // cP, cT convert velocity to displacement in cells (dt / (R sin(theta) h),
 // dt / (R h)); cP uses the grid point's latitude as the reference does.
+// The positions are formed by the same packed instructions as advect_from's,
+// so for a cell of rows 1 .. nTheta-3 away from the seam the two give the
+// same value wherever every sample of advect_from stays in its domain.
 template <int KIND>
 __device__ __forceinline__ float advect_cell(const float* __restrict__ u, const float* __restrict__ v,
                                              const float* __restrict__ field, int i, int j, float cP, float cT,
@@ -237,22 +246,17 @@ __device__ __forceinline__ float advect_cell(const float* __restrict__ u, const 
     constexpr float ov_p = cgp, ov_t = cgt - 1.0f;         // u_theta sampler
     // a field's own sampler offset equals its staggering: offset 0
     const bool vf = (g.flags & KAMINO_F_POLE_SIGN_FLIP) != 0;
-    float gu = sample_cell<KIND_VPHI>(u, i, j, ou_p, ou_t, g, vf);
-    float gv = sample_cell<KIND_VTHETA>(v, i, j, ov_p, ov_t, g, vf);
-    float dp = gu * cP, dtt = gv * cT;
-    float hp = 0.5f * dp, ht = 0.5f * dtt;
-    float mu = sample_cell<KIND_VPHI>(u, i, j, ou_p - hp, ou_t - ht, g, vf);
-    float mv = sample_cell<KIND_VTHETA>(v, i, j, ov_p - hp, ov_t - ht, g, vf);
-    dp = 0.5f * (mu + gu) * cP;
-    dtt = 0.5f * (mv + gv) * cT;
-    return sample_cell<KIND>(field, i, j, -dp, -dtt, g, vf && KIND != KIND_CENTERED);
+    const float2 gv = f2(sample_cell<KIND_VPHI>(u, i, j, ou_p, ou_t, g, vf),
+                         sample_cell<KIND_VTHETA>(v, i, j, ov_p, ov_t, g, vf));
+    const float2 nhc = __fmul2_rn(f2(cP, cT), f2(-0.5f, -0.5f));
+    const float2 hd = __fmul2_rn(gv, nhc);
+    const float2 pu = __fadd2_rn(hd, f2(ou_p, ou_t)), pv = __fadd2_rn(hd, f2(ov_p, ov_t));
+    const float mu = sample_cell<KIND_VPHI>(u, i, j, pu.x, pu.y, g, vf);
+    const float mv = sample_cell<KIND_VTHETA>(v, i, j, pv.x, pv.y, g, vf);
+    const float2 d = __fmul2_rn(__fadd2_rn(f2(mu, mv), gv), nhc);
+    return sample_cell<KIND>(field, i, j, d.x, d.y, g, vf && KIND != KIND_CENTERED);
 }
 
-// Packed pairs (f32x2: one instruction for two FP32 lanes of a register
-// pair, sm_100 and later) carry the two coordinates of a position and the
-// two row lerps of a bilinear sample.  Each lane rounds as the scalar
-// instruction would.
-__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
 // floor of a position pair by a round-down add of 1.5 * 2^23: t - 1.5 * 2^23
 // is floor(x) exactly for -2^22 <= x < 2^23, so the fraction x - floor(x) is
@@ -262,36 +266,40 @@ constexpr int kFloorBits = 0x4B400000;
 
 // sample_cell for positions whose rows it, it + 1 both lie in [0, pole_row)
 // and whose column pair does not straddle the phi seam: plain bilinear from
-// one address (the phi neighbour at +1, the next row at +pitch).  A pole
-// row, a crossing, the seam or a non-finite position goes to sample_cell,
-// so the result is sample_cell's for every phi offset of less than 2^22
-// cells (any displacement a stable time step can make).
+// one address (the phi neighbour at +1, the next row at +pitch), equal to
+// sample_cell's value there for every phi offset of less than 2^22 cells (any
+// displacement a stable time step can make).  Outside that domain (a pole
+// row, a crossing, the seam, a non-finite position) `bad` is set and the
+// value is meaningless; the reads still stay inside the field: the row is
+// clamped to pole_row - 1, so they touch rows 0 .. pole_row and, from the
+// last column, the first element of the row after (each field has two rows
+// past its data).
 // ib, jb = i, j - 0x4B400000 (mod 2^32): ib + bits(t) = i + floor(x).
 template <int KIND>
-__device__ __forceinline__ float sample_fast(const float* __restrict__ f, int i, int j, unsigned ib, unsigned jb,
-                                             float2 p, const KGeo& g, bool vec_flip)
+__device__ __forceinline__ float sample_try(const float* __restrict__ f, unsigned ib, unsigned jb, float2 p,
+                                            const KGeo& g, bool& bad)
 {
     const float2 t = __fadd2_rd(p, f2(kFloorBias, kFloorBias));
     const float2 a = __fadd2_rn(p, __ffma2_rn(t, f2(-1.0f, -1.0f), f2(kFloorBias, kFloorBias)));
-    const int it = (int)(jb + (unsigned)__float_as_int(t.y));
+    const unsigned it = jb + (unsigned)__float_as_int(t.y);
     const int i0 = (int)(ib + (unsigned)__float_as_int(t.x)) & g.mask;
-    const int pole_row = (KIND == KIND_VTHETA) ? g.nt - 2 : g.nt - 1;
-    if ((unsigned)it < (unsigned)pole_row && i0 != g.mask) {
-        const float* p0 = f + (it * g.pitch + i0);
-        const float* p1 = p0 + g.pitch;
-        const float2 lo = f2(__ldg(p0), __ldg(p1)), hi = f2(__ldg(p0 + 1), __ldg(p1 + 1));
-        const float2 r = __ffma2_rn(f2(a.x, a.x), __ffma2_rn(lo, f2(-1.0f, -1.0f), hi), lo);
-        return lerp2(r.x, r.y, a.y);
-    }
-    return sample_cell<KIND>(f, i, j, p.x, p.y, g, vec_flip);
+    const unsigned pole_row = (KIND == KIND_VTHETA) ? g.nt - 2 : g.nt - 1;
+    bad |= (it >= pole_row) | (i0 == g.mask);
+    const float* p0 = f + ((int)min(it, pole_row - 1) * g.pitch + i0);
+    const float* p1 = p0 + g.pitch;
+    const float2 lo = f2(__ldg(p0), __ldg(p1)), hi = f2(__ldg(p0 + 1), __ldg(p1 + 1));
+    const float2 r = __ffma2_rn(f2(a.x, a.x), __ffma2_rn(lo, f2(-1.0f, -1.0f), hi), lo);
+    return lerp2(r.x, r.y, a.y);
 }
 
 // RK2 step of one quantity from its start-point velocities gv = (u, v):
-// advect_cell after its first two samples.  nhc = (-cP / 2, -cT / 2).
+// advect_cell after its first two samples, through sample_try (`bad` set
+// when a sample left its domain; the caller then takes advect_cell).
+// nhc = (-cP / 2, -cT / 2).
 template <int KIND>
 __device__ __forceinline__ float advect_from(const float* __restrict__ u, const float* __restrict__ v,
-                                             const float* __restrict__ field, int i, int j, unsigned ib,
-                                             unsigned jb, float2 gv, float2 nhc, const KGeo& g, bool vf)
+                                             const float* __restrict__ field, unsigned ib, unsigned jb, float2 gv,
+                                             float2 nhc, const KGeo& g, bool& bad)
 {
     constexpr float cgp = (KIND == KIND_VPHI) ? -0.5f : 0.0f;
     constexpr float cgt = (KIND == KIND_VTHETA) ? 1.0f : 0.5f;
@@ -299,11 +307,11 @@ __device__ __forceinline__ float advect_from(const float* __restrict__ u, const 
     constexpr float ov_p = cgp, ov_t = cgt - 1.0f;
     // midpoint: offset - d / 2 for each sampler
     const float2 hd = __fmul2_rn(gv, nhc);
-    const float mu = sample_fast<KIND_VPHI>(u, i, j, ib, jb, __fadd2_rn(hd, f2(ou_p, ou_t)), g, vf);
-    const float mv = sample_fast<KIND_VTHETA>(v, i, j, ib, jb, __fadd2_rn(hd, f2(ov_p, ov_t)), g, vf);
+    const float mu = sample_try<KIND_VPHI>(u, ib, jb, __fadd2_rn(hd, f2(ou_p, ou_t)), g, bad);
+    const float mv = sample_try<KIND_VTHETA>(v, ib, jb, __fadd2_rn(hd, f2(ov_p, ov_t)), g, bad);
     // departure point: -(mid + start) / 2 * c
     const float2 d = __fmul2_rn(__fadd2_rn(f2(mu, mv), gv), nhc);
-    return sample_fast<KIND>(field, i, j, ib, jb, d, g, vf && KIND != KIND_CENTERED);
+    return sample_try<KIND>(field, ib, jb, d, g, bad);
 }
 
 // The three advected quantities of cell (i, j) in one thread: u_phi at
@@ -315,7 +323,12 @@ __device__ __forceinline__ float advect_from(const float* __restrict__ u, const 
 //   u_theta point:  u = bilinear of u[j..j+1][i..i+1],  v = v[j][i]
 //   centred point:  u = mean of u[j][i..i+1],  v = mean of v[j-1..j][i]
 // The rows next to the poles and the two columns at the phi seam run
-// advect_cell for each quantity.
+// advect_cell for each quantity, and so does a cell one of whose samples left
+// sample_try's domain (its fast values are discarded), with one copy of the
+// exact path in the kernel.  advect_cell forms its positions with
+// advect_from's instructions and sample_cell equals sample_try inside the
+// domain, so a quantity whose samples all stayed inside it gets the same
+// value either way.
 // MASK selects the quantities (bit 0 u_phi, bit 1 u_theta, bit 2 thickness);
 // each one's value does not depend on which others are computed.
 template <int MASK = 7>
@@ -323,7 +336,7 @@ __device__ __forceinline__ void advect_cell3(const float* __restrict__ u, const 
                                              const float* __restrict__ rho, int i, int j, float cPc, float cPv,
                                              float cT, const KGeo& g, float& out_u, float& out_v, float& out_r)
 {
-    const bool vf = (g.flags & KAMINO_F_POLE_SIGN_FLIP) != 0;
+    bool exact = true;
     if (j >= 1 && j <= g.nt - 3 && i >= 1 && i < g.mask) {
         // columns i - 1 .. i + 1 without wrapping: neighbours at +-1
         const float* uj = u + (j * g.pitch + i);
@@ -344,18 +357,21 @@ __device__ __forceinline__ void advect_cell3(const float* __restrict__ u, const 
         const unsigned ib = (unsigned)i - (unsigned)kFloorBits, jb = (unsigned)j - (unsigned)kFloorBits;
         const float2 nhc = __fmul2_rn(f2(cPc, cT), f2(-0.5f, -0.5f));
         const float2 nhv = f2(-0.5f * cPv, nhc.y);
+        bool bad = false;
         if constexpr ((MASK & 1) != 0)
-            out_u = advect_from<KIND_VPHI>(u, v, u, i, j, ib, jb, f2(gu_phi, gv_phi), nhc, g, vf);
+            out_u = advect_from<KIND_VPHI>(u, v, u, ib, jb, f2(gu_phi, gv_phi), nhc, g, bad);
         if constexpr ((MASK & 2) != 0)
-            out_v = advect_from<KIND_VTHETA>(u, v, v, i, j, ib, jb, f2(gu_th, gv_th), nhv, g, vf);
+            out_v = advect_from<KIND_VTHETA>(u, v, v, ib, jb, f2(gu_th, gv_th), nhv, g, bad);
         if constexpr ((MASK & 4) != 0)
-            out_r = advect_from<KIND_CENTERED>(u, v, rho, i, j, ib, jb, f2(gu_c, gv_c), nhc, g, vf);
-        return;
+            out_r = advect_from<KIND_CENTERED>(u, v, rho, ib, jb, f2(gu_c, gv_c), nhc, g, bad);
+        exact = bad;
     }
-    if constexpr ((MASK & 1) != 0) out_u = advect_cell<KIND_VPHI>(u, v, u, i, j, cPc, cT, g);
-    if constexpr ((MASK & 2) != 0)
-        if (j < g.nt - 1) out_v = advect_cell<KIND_VTHETA>(u, v, v, i, j, cPv, cT, g);
-    if constexpr ((MASK & 4) != 0) out_r = advect_cell<KIND_CENTERED>(u, v, rho, i, j, cPc, cT, g);
+    if (exact) {
+        if constexpr ((MASK & 1) != 0) out_u = advect_cell<KIND_VPHI>(u, v, u, i, j, cPc, cT, g);
+        if constexpr ((MASK & 2) != 0)
+            if (j < g.nt - 1) out_v = advect_cell<KIND_VTHETA>(u, v, v, i, j, cPv, cT, g);
+        if constexpr ((MASK & 4) != 0) out_r = advect_cell<KIND_CENTERED>(u, v, rho, i, j, cPc, cT, g);
+    }
 }
 
 // PTX rcp.approx.ftz.f32: the hardware reciprocal, within about an ulp.
