@@ -119,6 +119,13 @@ __device__ __forceinline__ void advect_particle(const KGeo& g, const float* __re
     out = make_float2(updatedPhi, updatedTheta);
 }
 
+// Threads of the cell-exact advection: one per cell in row order, where the
+// two seam columns (i = 0 and nPhi-1) are skipped, then 2 nTheta more that
+// take the seam cells of every row.  The seam cells always run the exact
+// path, so they fill warps of their own instead of making the first and last
+// warp of every row diverge; the row-order warps stay aligned to 32 cells.
+__host__ __device__ inline int adv_cell_threads(const KGeo& g) { return g.nt * g.np + 2 * g.nt; }
+
 // Advection tiles of one sphere: the cell-exact kernel takes one cell per
 // thread and advects its three quantities (nb_u tiles, nb_v = nb_r = 0); the
 // reference-rounding kernel takes one point per thread, nb_u tiles of u_phi,
@@ -127,13 +134,29 @@ __device__ __forceinline__ void advect_particle(const KGeo& g, const float* __re
 inline void adv_tiles(const KGeo& g, int& nb_u, int& nb_v, int& nb_r)
 {
     const int T = ADV_THREADS;
-    nb_u = (g.nt * g.np + T - 1) / T;
     if (g.flags & KAMINO_F_REFERENCE_ROUNDING) {
+        nb_u = (g.nt * g.np + T - 1) / T;
         nb_v = ((g.nt - 1) * g.np + T - 1) / T;
         nb_r = nb_u;
     } else {
+        nb_u = (adv_cell_threads(g) + T - 1) / T;
         nb_v = nb_r = 0;
     }
+}
+
+// Cell (i, j) of cell-exact advection thread t; false: the thread has none.
+__device__ __forceinline__ bool adv_cell_of(const KGeo& g, int t, int& i, int& j)
+{
+    const int n = g.nt * g.np;
+    if (t < n) {
+        j = t >> (g.log2nt + 1);
+        i = t & g.mask;
+        return i != 0 && i != g.mask;
+    }
+    const int k = t - n;
+    j = k >> 1;
+    i = (k & 1) ? g.mask : 0;
+    return k < 2 * g.nt;
 }
 
 // Cell tile `blk` of the cell-exact advection (one cell per thread, its three
@@ -145,9 +168,9 @@ __device__ __forceinline__ void advect_cells_tile(const KGeo& g, const float* __
                                                   float* __restrict__ ro, const float* __restrict__ cell_c,
                                                   const float* __restrict__ cell_v, int blk, int tid)
 {
-    const int idx = blk * ADV_THREADS + tid;
-    if (idx >= g.nt * g.np) return;
-    const int j = idx >> (g.log2nt + 1), i = idx & g.mask;
+    int i, j;
+    if (!adv_cell_of(g, blk * ADV_THREADS + tid, i, j)) return;
+    const int idx = (j << (g.log2nt + 1)) + i;
     float ou, ov = 0.0f, orr;
     advect_cell3(u, v, rho, i, j, __ldg(cell_c + j), __ldg(cell_v + j), g.cellTheta, g, ou, ov, orr);
     uo[idx] = ou;
@@ -223,9 +246,9 @@ __global__ void __launch_bounds__(ADV_THREADS, 8) k_advect_part(KGeo g, KBufs b,
     int blk = blockIdx.x;
     const int tid = threadIdx.x;
     if (blk < nb_u) {
-        const int idx = blk * ADV_THREADS + tid;
-        if (idx >= g.nt * g.np) return;
-        const int j = idx >> (g.log2nt + 1), i = idx & g.mask;
+        int i, j;
+        if (!adv_cell_of(g, blk * ADV_THREADS + tid, i, j)) return;
+        const int idx = (j << (g.log2nt + 1)) + i;
         float ou = 0.0f, ov = 0.0f, orr = 0.0f;
         advect_cell3<MASK>(u, v, b.rho[sr], i, j, __ldg(b.cell_c + j), __ldg(b.cell_v + j), g.cellTheta, g, ou, ov,
                            orr);

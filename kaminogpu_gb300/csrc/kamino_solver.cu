@@ -532,7 +532,7 @@ static int enqueue_step(kamino_solver_s* h, int cu, int cr, cudaEvent_t* ev, cud
     if (!rc && io) {
         const KGeo& g = h->g;
         const int T = kk::ADV_THREADS;
-        const int nb_u = (g.nt * g.np + T - 1) / T, nb_p = (int)((h->b.npart + T - 1) / T);
+        const int nb_u = (kk::adv_cell_threads(g) + T - 1) / T, nb_p = (int)((h->b.npart + T - 1) / T);
         cudaError_t e = kk::launch_pdl(kk::k_advect_part<3>, nb_u + nb_p, T, 0, h->stream, g, h->b, cu, 1 - cu, cr,
                                        1 - cr, nb_u);
         rc = launched("k_advect_part<3>", e);
