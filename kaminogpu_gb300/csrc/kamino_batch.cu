@@ -81,6 +81,7 @@ __global__ void __launch_bounds__(kk::ADV_THREADS, 8) kb_advect(const KSphere* _
     __shared__ KSphere s;
     __shared__ int s_item;
     int2 w;
+    kk::pdl_wait();
     while (next_item(counter, n, items, sph, tiles_per_item, &s, &s_item, &w)) {
         const int t0 = w.y * tiles_per_item, t1 = min(t0 + tiles_per_item, s.nb_adv);
         if constexpr (CELLS) {
@@ -89,13 +90,13 @@ __global__ void __launch_bounds__(kk::ADV_THREADS, 8) kb_advect(const KSphere* _
             const float *u = s.b.u[cu], *v = s.b.v[cu], *rho = s.b.rho[cr], *cc = s.b.cell_c, *cv = s.b.cell_v;
             float *uo = s.b.u[1 - cu], *vo = s.b.v[1 - cu], *ro = s.b.rho[1 - cr];
             for (int t = t0; t < t1; t++) kk::advect_cells_tile(g, u, v, rho, uo, vo, ro, cc, cv, t, threadIdx.x);
-            continue;
-        }
-        for (int t = t0; t < t1; t++) {
-            if (s.ref)
-                kk::advect_tile<true>(s.g, s.b, cu, 1 - cu, cr, 1 - cr, s.nb_u, s.nb_v, s.nb_r, t, threadIdx.x);
-            else
-                kk::advect_tile<false>(s.g, s.b, cu, 1 - cu, cr, 1 - cr, s.nb_u, s.nb_v, s.nb_r, t, threadIdx.x);
+        } else {
+            for (int t = t0; t < t1; t++) {
+                if (s.ref)
+                    kk::advect_tile<true>(s.g, s.b, cu, 1 - cu, cr, 1 - cr, s.nb_u, s.nb_v, s.nb_r, t, threadIdx.x);
+                else
+                    kk::advect_tile<false>(s.g, s.b, cu, 1 - cu, cr, 1 - cr, s.nb_u, s.nb_v, s.nb_r, t, threadIdx.x);
+            }
         }
     }
 }
@@ -107,6 +108,7 @@ __global__ void __launch_bounds__(kk::ELEM_THREADS) kb_geo(const KSphere* __rest
     __shared__ KSphere s;
     __shared__ int s_item;
     int2 w;
+    kk::pdl_wait();
     while (next_item(counter, n, items, sph, tiles_per_item, &s, &s_item, &w)) {
         const int t0 = w.y * tiles_per_item, t1 = min(t0 + tiles_per_item, s.nb_elem);
         for (int t = t0; t < t1; t++) kk::geo_tile(s.g, s.b, src, t * kk::ELEM_THREADS + threadIdx.x);
@@ -127,6 +129,7 @@ __global__ void __launch_bounds__(kk::FFT_MAX_THREADS, fft_stage_min_ctas(MAXN))
     __shared__ KSphere s;
     __shared__ int s_item;
     int2 w;
+    kk::pdl_wait();
     while (next_item(counter, n, items, sph, 1, &s, &s_item, &w))
         kk::div_fft_tile<0, MAXN>(s.g, s.b, uv_in, uv_out, w.y, threadIdx.x, sm2);
 }
@@ -139,6 +142,7 @@ __global__ void __launch_bounds__(kk::SOLVE_THREADS) kb_solve(const KSphere* __r
     __shared__ KSphere s;
     __shared__ int s_item;
     int2 w;
+    kk::pdl_wait();
     while (next_item(counter, n, items, sph, 1, &s, &s_item, &w))
         kk::solve_tile<MAXN>(s.g, s.b, s.nfp64, w.y, threadIdx.x, smraw);
 }
@@ -152,6 +156,7 @@ __global__ void __launch_bounds__(kk::FFT_MAX_THREADS, fft_stage_min_ctas(MAXN))
     __shared__ KSphere s;
     __shared__ int s_item;
     int2 w;
+    kk::pdl_wait();
     while (next_item(counter, n, items, sph, 1, &s, &s_item, &w))
         kk::ifft_tile<MAXN>(s.g, s.b, uv_in, uv_out, w.y, threadIdx.x, sm2);
 }
@@ -172,6 +177,7 @@ __global__ void __launch_bounds__(kk::ELEM_THREADS) kb_vgrad(const KSphere* __re
     __shared__ KSphere s;
     __shared__ int s_item;
     int2 w;
+    kk::pdl_wait();
     while (next_item(counter, n, items, sph, tiles_per_item, &s, &s_item, &w)) {
         const int t0 = w.y * tiles_per_item, t1 = min(t0 + tiles_per_item, s.nb_elem);
         for (int t = t0; t < t1; t++) kk::vgrad_tile(s.g, s.b, uv_in, uv_out, t * kk::ELEM_THREADS + threadIdx.x);
@@ -367,20 +373,25 @@ struct Engine {
     {
         BCUDA(cudaMemsetAsync(d_counters, 0, sizeof(int) * ST_COUNT, stream));
         const int tpi = std::max(1, shapes.adv_tiles_per_item);
-        (cells_only ? kb_advect<true> : kb_advect<false>)<<<grid(ST_ADV), kk::ADV_THREADS, 0, stream>>>(
-            d_desc, d_items + item_off[ST_ADV], n_items[ST_ADV], d_counters + ST_ADV, c, r, tpi);
-        kb_geo<<<grid(ST_GEO), kk::ELEM_THREADS, 0, stream>>>(d_desc, d_items + item_off[ST_GEO], n_items[ST_GEO],
-                                                               d_counters + ST_GEO, 1 - c, tpi);
-        div_stage(cls)<<<grid(ST_DIV), fft_block, smem_fft, stream>>>(d_desc, d_items + item_off[ST_DIV],
-                                                                       n_items[ST_DIV], d_counters + ST_DIV, 1 - c, c);
-        solve_stage(cls)<<<grid(ST_SOLVE), kk::SOLVE_THREADS, smem_solve, stream>>>(
-            d_desc, d_items + item_off[ST_SOLVE], n_items[ST_SOLVE], d_counters + ST_SOLVE);
-        ifft_stage(cls)<<<grid(ST_IFFT), fft_block, smem_fft, stream>>>(d_desc, d_items + item_off[ST_IFFT],
-                                                                        n_items[ST_IFFT], d_counters + ST_IFFT, c,
-                                                                        1 - c);
-        kb_vgrad<<<grid(ST_VGRAD), kk::ELEM_THREADS, 0, stream>>>(d_desc, d_items + item_off[ST_VGRAD],
-                                                                   n_items[ST_VGRAD], d_counters + ST_VGRAD, c, 1 - c,
-                                                                   tpi);
+        // programmatic dependent launches: each stage's CTAs are scheduled as
+        // the previous stage's finish and wait in pdl_wait for all of it
+        const KSphere* D = d_desc;
+        BCUDA(kk::launch_pdl(cells_only ? kb_advect<true> : kb_advect<false>, grid(ST_ADV), kk::ADV_THREADS, 0,
+                             stream, D, (const int2*)(d_items + item_off[ST_ADV]), n_items[ST_ADV],
+                             d_counters + ST_ADV, c, r, tpi));
+        BCUDA(kk::launch_pdl(kb_geo, grid(ST_GEO), kk::ELEM_THREADS, 0, stream, D,
+                             (const int2*)(d_items + item_off[ST_GEO]), n_items[ST_GEO], d_counters + ST_GEO, 1 - c,
+                             tpi));
+        BCUDA(kk::launch_pdl(div_stage(cls), grid(ST_DIV), fft_block, smem_fft, stream, D,
+                             (const int2*)(d_items + item_off[ST_DIV]), n_items[ST_DIV], d_counters + ST_DIV, 1 - c, c));
+        BCUDA(kk::launch_pdl(solve_stage(cls), grid(ST_SOLVE), kk::SOLVE_THREADS, smem_solve, stream, D,
+                             (const int2*)(d_items + item_off[ST_SOLVE]), n_items[ST_SOLVE], d_counters + ST_SOLVE));
+        BCUDA(kk::launch_pdl(ifft_stage(cls), grid(ST_IFFT), fft_block, smem_fft, stream, D,
+                             (const int2*)(d_items + item_off[ST_IFFT]), n_items[ST_IFFT], d_counters + ST_IFFT, c,
+                             1 - c));
+        BCUDA(kk::launch_pdl(kb_vgrad, grid(ST_VGRAD), kk::ELEM_THREADS, 0, stream, D,
+                             (const int2*)(d_items + item_off[ST_VGRAD]), n_items[ST_VGRAD], d_counters + ST_VGRAD, c,
+                             1 - c, tpi));
         BCUDA(cudaGetLastError());
         return KAMINO_OK;
     }
