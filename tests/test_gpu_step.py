@@ -285,6 +285,44 @@ def test_step_host_matches_separate_calls_bitwise(kg, orc, nt, npart, ref):
     assert np.array_equal(r, want["thickness"])
 
 
+@pytest.mark.parametrize("nt", [64, 256])
+def test_fast_sampler_flags_at_high_velocity(kg, orc, nt):
+    """Velocity x3 with a vortex: the rows next to the poles move many cells
+    in phi per step, so many cells have a sample across a pole or at the phi
+    seam; the advection's fast sampler flags them and the whole cell takes
+    the exact path.  One advection stage against the FP64 oracle (with the
+    pole sign flip, so the sampler is continuous across the pole), and the
+    host-buffer step, whose u_phi/u_theta and thickness advections are two
+    launches that flag only their own quantities, against the one-launch
+    step bit for bit, with and without the sign flip."""
+    st = kg.make_initial_state(nt, lmax=8, seed=21, radius=0.8, vortex=True, velocity_scale=3.0)
+    flip = kg.F_POLE_SIGN_FLIP
+    cfg = kg.default_config(n_theta=nt, radius=0.8, dt=0.004, flags=flip)
+    with kg.KaminoSolver(config=cfg) as s:
+        s.load(st)
+        s.advection()
+        got = s.fields()
+    o = orc.Oracle(nt, 0.8, 0.004, flip, 0)
+    o.load(st)
+    o.advection()
+    want = o.fields()
+    for k in FIELDS:
+        err = orc.rel_l2(got[k], want[k])
+        assert err <= TOL, "%s after the advection at velocity x3: rel L2 %.3e" % (k, err)
+    for flags in (0, flip):
+        cfg = kg.default_config(n_theta=nt, radius=0.8, dt=0.004, flags=flags)
+        with kg.KaminoSolver(config=cfg) as a, kg.KaminoSolver(config=cfg) as b:
+            u, v, r = st["u_phi"], st["u_theta"], st["thickness"]
+            b.load(st)
+            for _ in range(3):
+                u, v, r = a.step_host(u, v, r)
+                b.stepForward()
+            want = b.fields()
+        assert np.array_equal(u, want["u_phi"]), flags
+        assert np.array_equal(v, want["u_theta"]), flags
+        assert np.array_equal(r, want["thickness"]), flags
+
+
 def test_mid_size_with_particles(kg, orc):
     """The mid-size configuration: nTheta=512 x nPhi=1024, radius 1,
     dt=0.002, l<=16, 2^20 particles advected with RK2.  Fields and particles
