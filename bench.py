@@ -19,9 +19,11 @@ e2e:   the same steps through the public C ABI with host buffers: every step
   threads) on the same configuration, from the same seeded state made by the
   oracle's own generator (the product library is never loaded there), plus
   the reference's own CUDA kernels on this GPU as extra information.
-Extra keys of the GPU arm: config2 (nTheta=512 with 2^20 RK2 particles),
-  batched (256 spheres), served (closed loop, and Poisson arrivals at 200/s
-  for --served-seconds, 60 by default), frame_output, cpu_baseline.
+Extra keys of the GPU arm: fp64_modes_0 (every mode in FP32),
+  reference_rounding (the same step with the reference's own sampler
+  arithmetic, bit-exact index map), config2 (nTheta=512 with 2^20 RK2
+  particles), batched (256 spheres), served (closed loop, and Poisson arrivals
+  at 200/s for --served-seconds, 60 by default), frame_output, cpu_baseline.
 With N > 1 (torchrun), every rank advances its own sphere (replicas; the
 path does not shard) and rank 0 prints the aggregate.
 """
@@ -271,6 +273,7 @@ def run_ours(args, ws, rank, local, dist):
         "clocks": ck.summary(),
     }
     out["fp64_modes_0"] = bench_fp64_modes_0(kg, local, st, steps=min(args.steps, 500))
+    out["reference_rounding"] = bench_reference_rounding(kg, local, st, steps=min(args.steps, 500))
     if not args.no_config2:
         out["config2"] = bench_particles(kg, local, hbm)
     if not args.no_batched:
@@ -299,6 +302,26 @@ def bench_fp64_modes_0(kg, local, st, steps):
         ms = s.time_steps(steps, flush_l2=True) / steps
     return {"ms_per_step": ms, "cell_steps_per_s": NT * 2 * NT / (ms / 1e3), "k_solve_ms": kms["k_solve"],
             "what": "fp64_modes=0: every mode solved in FP32, %d timed steps" % steps}
+
+
+def bench_reference_rounding(kg, local, st, steps):
+    """The same sphere with KAMINO_F_REFERENCE_ROUNDING: the samplers in
+    radians with the reference's own rounding, whose pole-wrap index map is
+    bit-exact with the reference's validateCoord (the drop-in's exact mode)."""
+    cfg = kg.default_config(n_theta=NT, radius=1.0, dt=DT, fp64_modes=4, flags=kg.F_REFERENCE_ROUNDING, device=local)
+    with kg.KaminoSolver(config=cfg) as s:
+        s.load(st)
+        s.step_n(5)
+        s.synchronize()
+        kms = s.time_kernels(reps=10, flush_l2=True)
+        s.load(st)
+        s.step_n(3)
+        s.synchronize()
+        ms = s.time_steps(steps, flush_l2=True) / steps
+    return {"ms_per_step": ms, "cell_steps_per_s": NT * 2 * NT / (ms / 1e3), "k_advect_ms": kms["k_advect"],
+            "kernel_ms": kms,
+            "what": "KAMINO_F_REFERENCE_ROUNDING (radian samplers, the reference's index arithmetic bit for bit), "
+                    "%d timed steps" % steps}
 
 
 def bench_particles(kg, local, hbm, npart=1 << 20, steps=200):

@@ -152,6 +152,59 @@ __device__ __forceinline__ float advect_point(const float* __restrict__ u, const
     return sample<KIND>(field, pPhi, pTheta, g, vf && KIND != KIND_CENTERED);
 }
 
+// sample() for a position that needs no wrap (validateCoord leaves it
+// untouched) and is not in a pole row, with no branch: `bad` is set for any
+// other position, whose value is then meaningless; the row is clamped, so
+// the reads stay inside the field whatever the position.  Where `bad` stays
+// clear the operations are sample()'s own, so the value is the same.
+template <int KIND>
+__device__ __forceinline__ float sample_ref_try(const float* __restrict__ f, float phiRaw, float thetaRaw,
+                                            const KGeo& g, bool& bad)
+{
+    const float phi = (KIND == KIND_VPHI) ? __fadd_rn(phiRaw, g.halfh) : phiRaw;
+    const float theta = (KIND == KIND_VTHETA) ? __fsub_rn(thetaRaw, g.h) : __fsub_rn(thetaRaw, g.halfh);
+    bad |= !(theta >= 0.0f && theta < g.pi_up && phi >= 0.0f && phi < g.wrap_phi_hi);
+    const float nphi = __fmul_rn(phi, g.invh), nth = __fmul_rn(theta, g.invh);
+    const float fp = floorf(nphi), ft = floorf(nth);
+    const float ap = __fsub_rn(nphi, __fadd_rn(fp, 0.0f));
+    const float at = __fsub_rn(nth, __fadd_rn(ft, 0.0f));
+    const int i0 = ((int)fp) & g.mask, i1 = (i0 + 1) & g.mask;
+    const unsigned pole_row = (KIND == KIND_VTHETA) ? g.nt - 2 : g.nt - 1;
+    const unsigned it = (unsigned)(int)ft;
+    bad |= it >= pole_row;
+    const float* r0 = f + (size_t)min(it, pole_row - 1) * g.pitch;
+    const float* r1 = r0 + g.pitch;
+    const float v00 = __ldg(r0 + i0), v01 = __ldg(r0 + i1), v10 = __ldg(r1 + i0), v11 = __ldg(r1 + i1);
+    return klerp(klerp(v00, v01, ap), klerp(v10, v11, ap), at);
+}
+
+// advect_point through sample_ref_try: a point one of whose five samples
+// needs a wrap or lies in a pole row is recomputed by advect_point, so the
+// value is advect_point's in every case.
+template <int KIND>
+__device__ __forceinline__ float advect_point_fast(const float* __restrict__ u, const float* __restrict__ v,
+                                                   const float* __restrict__ field, float gPhi, float gTheta,
+                                                   float cofPhi, const KGeo& g)
+{
+    bool bad = false;
+    const float guPhi = sample_ref_try<KIND_VPHI>(u, gPhi, gTheta, g, bad);
+    const float guTheta = sample_ref_try<KIND_VTHETA>(v, gPhi, gTheta, g, bad);
+    float deltaPhi = __fmul_rn(guPhi, cofPhi);
+    float deltaTheta = __fmul_rn(guTheta, g.cofTheta);
+    const float midPhi = __fsub_rn(gPhi, 0.5f * deltaPhi);
+    const float midTheta = __fsub_rn(gTheta, 0.5f * deltaTheta);
+    const float muPhi = sample_ref_try<KIND_VPHI>(u, midPhi, midTheta, g, bad);
+    const float muTheta = sample_ref_try<KIND_VTHETA>(v, midPhi, midTheta, g, bad);
+    const float averuPhi = 0.5f * __fadd_rn(muPhi, guPhi);
+    const float averuTheta = 0.5f * __fadd_rn(muTheta, guTheta);
+    deltaPhi = __fmul_rn(averuPhi, cofPhi);
+    deltaTheta = __fmul_rn(averuTheta, g.cofTheta);
+    const float pPhi = __fsub_rn(gPhi, deltaPhi);
+    const float pTheta = __fsub_rn(gTheta, deltaTheta);
+    const float r = sample_ref_try<KIND>(field, pPhi, pTheta, g, bad);
+    return bad ? advect_point<KIND>(u, v, field, gPhi, gTheta, cofPhi, g) : r;
+}
+
 // ------------------------------------------------- cell-exact positions
 // A position is a grid point (i, j) plus a small FP32 offset (fp, ft) in
 // cells, so the integer part is exact and the fraction keeps full relative

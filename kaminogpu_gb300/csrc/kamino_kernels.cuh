@@ -124,6 +124,8 @@ __device__ __forceinline__ void advect_particle(const KGeo& g, const float* __re
 // take the seam cells of every row.  The seam cells always run the exact
 // path, so they fill warps of their own instead of making the first and last
 // warp of every row diverge; the row-order warps stay aligned to 32 cells.
+// (The reference-rounding tiles keep plain row order: the same split spilled
+// their registers and lost at nTheta = 1024.)
 __host__ __device__ inline int adv_cell_threads(const KGeo& g) { return g.nt * g.np + 2 * g.nt; }
 
 // Advection tiles of one sphere: the cell-exact kernel takes one cell per
@@ -194,19 +196,19 @@ __device__ __forceinline__ void advect_tile(const KGeo& g, const KBufs& b, int s
     if (REF && blk < nb_u + nb_v + nb_r) {
         const int which = blk < nb_u ? 0 : (blk < nb_u + nb_v ? 1 : 2);
         const int b0 = which == 0 ? 0 : (which == 1 ? nb_u : nb_u + nb_v);
-        int idx = (blk - b0) * ADV_THREADS + tid;
+        const int idx = (blk - b0) * ADV_THREADS + tid;
         if (idx >= (which == 1 ? g.nt - 1 : g.nt) * g.np) return;
-        int j = idx >> lg, i = idx & g.mask;
+        const int j = idx >> lg, i = idx & g.mask;
         float val;
         if (which == 0) {
             float gPhi = __fmul_rn((float)i - 0.5f, g.h), gTheta = __fmul_rn((float)j + 0.5f, g.h);
-            val = advect_point<KIND_VPHI>(u, v, u, gPhi, gTheta, __ldg(b.cof_c + j), g);
+            val = advect_point_fast<KIND_VPHI>(u, v, u, gPhi, gTheta, __ldg(b.cof_c + j), g);
         } else if (which == 1) {
             float gPhi = __fmul_rn((float)i, g.h), gTheta = __fmul_rn((float)j + 1.0f, g.h);
-            val = advect_point<KIND_VTHETA>(u, v, v, gPhi, gTheta, __ldg(b.cof_v + j), g);
+            val = advect_point_fast<KIND_VTHETA>(u, v, v, gPhi, gTheta, __ldg(b.cof_v + j), g);
         } else {
             float gPhi = __fmul_rn((float)i, g.h), gTheta = __fmul_rn((float)j + 0.5f, g.h);
-            val = advect_point<KIND_CENTERED>(u, v, b.rho[sr], gPhi, gTheta, __ldg(b.cof_c + j), g);
+            val = advect_point_fast<KIND_CENTERED>(u, v, b.rho[sr], gPhi, gTheta, __ldg(b.cof_c + j), g);
         }
         float* dst = which == 0 ? b.u[duv] : (which == 1 ? b.v[duv] : b.rho[dr]);
         dst[idx] = val;
