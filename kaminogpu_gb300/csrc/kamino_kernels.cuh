@@ -119,6 +119,43 @@ __device__ __forceinline__ void advect_particle(const KGeo& g, const float* __re
     out = make_float2(updatedPhi, updatedTheta);
 }
 
+// advect_particle through sample_ref_try: a particle with a sample that
+// needs a wrap or lies in a pole row, or whose midpoint or new position
+// needs validateCoord's wrap, is recomputed by advect_particle; otherwise
+// the operations are advect_particle's own, so the result is the same.
+__device__ __forceinline__ void advect_particle_fast(const KGeo& g, const float* __restrict__ u,
+                                                     const float* __restrict__ v, float2 pos, float2& out)
+{
+    bool bad = false;
+    const float posPhi = pos.x, posTheta = pos.y;
+    const float uPhi = sample_ref_try<KIND_VPHI>(u, posPhi, posTheta, g, bad);
+    const float uTheta = sample_ref_try<KIND_VTHETA>(v, posPhi, posTheta, g, bad);
+    const float latRadius = __fmul_rn(g.R, sinf(posTheta));
+    const float cofPhi = __fdiv_rn(g.dt, latRadius);
+    float updatedTheta, updatedPhi;
+    if (!(g.flags & KAMINO_F_PARTICLE_RK2)) {
+        updatedTheta = __fadd_rn(posTheta, __fmul_rn(uTheta, g.cofTheta));
+        updatedPhi = posPhi;
+        if (latRadius > 1e-7f) updatedPhi = __fadd_rn(posPhi, __fmul_rn(uPhi, cofPhi));
+    } else {
+        const float midTheta = __fadd_rn(posTheta, __fmul_rn(0.5f * uTheta, g.cofTheta));
+        float midPhi = posPhi;
+        if (latRadius > 1e-7f) midPhi = __fadd_rn(posPhi, __fmul_rn(0.5f * uPhi, cofPhi));
+        bad |= !(midTheta >= 0.0f && midTheta < g.pi_up && midPhi >= 0.0f && midPhi < g.wrap_phi_hi);
+        const float mPhi = sample_ref_try<KIND_VPHI>(u, midPhi, midTheta, g, bad);
+        const float mTheta = sample_ref_try<KIND_VTHETA>(v, midPhi, midTheta, g, bad);
+        const float latMid = __fmul_rn(g.R, sinf(midTheta));
+        updatedTheta = __fadd_rn(posTheta, __fmul_rn(mTheta, g.cofTheta));
+        updatedPhi = posPhi;
+        if (latMid > 1e-7f) updatedPhi = __fadd_rn(posPhi, __fmul_rn(mPhi, __fdiv_rn(g.dt, latMid)));
+    }
+    bad |= !(updatedTheta >= 0.0f && updatedTheta < g.pi_up && updatedPhi >= 0.0f && updatedPhi < g.wrap_phi_hi);
+    if (bad)
+        advect_particle(g, u, v, pos, out);
+    else
+        out = make_float2(updatedPhi, updatedTheta);
+}
+
 // Threads of the cell-exact advection: one per cell in row order, where the
 // two seam columns (i = 0 and nPhi-1) are skipped, then 2 nTheta more that
 // take the seam cells of every row.  The seam cells always run the exact
@@ -219,7 +256,7 @@ __device__ __forceinline__ void advect_tile(const KGeo& g, const KBufs& b, int s
     if (k >= b.npart) return;
     if (b.pperm) k = __ldg(b.pperm + k);  // the particle this thread takes
     float2 out;
-    advect_particle(g, u, v, b.part[sr][k], out);
+    advect_particle_fast(g, u, v, b.part[sr][k], out);
     b.part[dr][k] = out;
 }
 
@@ -265,7 +302,7 @@ __global__ void __launch_bounds__(ADV_THREADS, 8) k_advect_part(KGeo g, KBufs b,
         if (k >= b.npart) return;
         if (b.pperm) k = __ldg(b.pperm + k);
         float2 out;
-        advect_particle(g, u, v, b.part[sr][k], out);
+        advect_particle_fast(g, u, v, b.part[sr][k], out);
         b.part[dr][k] = out;
     }
 }
