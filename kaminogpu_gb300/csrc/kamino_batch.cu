@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(kk::ADV_THREADS, 8) kb_advect(const KSphere* _
     }
 }
 
-__global__ void __launch_bounds__(kk::ELEM_THREADS) kb_geo(const KSphere* __restrict__ sph,
+__global__ void __launch_bounds__(kk::ELEM_THREADS, 8) kb_geo(const KSphere* __restrict__ sph,
                                                             const int2* __restrict__ items, int n, int* counter,
                                                             int src, int tiles_per_item)
 {
@@ -115,6 +115,12 @@ __global__ void __launch_bounds__(kk::ELEM_THREADS) kb_geo(const KSphere* __rest
     }
 }
 
+// kb_geo and the 256 class of kb_solve are compiled for eight resident CTAs
+// per SM (32 and 64 registers, a few bytes spilled): a persistent stage
+// drains its queue faster with more CTAs in flight than with the registers
+// that would avoid the spills (0.458 -> 0.442 ms per step on the 256-sphere
+// mix, against 60 and 94 registers).
+//
 // The FFT and solve stages come in two instances by the batch's largest
 // nTheta (MAXN = 256, 1024; batched spheres have nTheta <= 1024): a batch of
 // small spheres does not run code sized, in registers, for the 1024-row
@@ -135,7 +141,7 @@ __global__ void __launch_bounds__(kk::FFT_MAX_THREADS, fft_stage_min_ctas(MAXN))
 }
 
 template <int MAXN>
-__global__ void __launch_bounds__(kk::SOLVE_THREADS) kb_solve(const KSphere* __restrict__ sph,
+__global__ void __launch_bounds__(kk::SOLVE_THREADS, MAXN <= 256 ? 8 : 1) kb_solve(const KSphere* __restrict__ sph,
                                                                const int2* __restrict__ items, int n, int* counter)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
