@@ -407,8 +407,9 @@ __device__ __forceinline__ float2 shfl2(float2 v, int src, int width)
 // spectrum and solution columns it exchanges with global memory are whole
 // 32-byte sectors (R rows x 8 bytes), staged in shared memory with the row
 // index fastest.  The transpose blocks and the staging area share the
-// dynamic shared memory; a CTA barrier separates their uses.  At N = 1024
-// the CTA has twice the warps its rows' transforms need (the *_w8 tiles).
+// dynamic shared memory; a CTA barrier separates their uses.  At N = 512
+// and 1024 the CTA has 8 warps, more than its rows' transforms need (the
+// *_w8 tiles).
 __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n >> 1); }
 __host__ __device__ constexpr int brev(int i, int bits)
 {
@@ -418,11 +419,11 @@ __host__ __device__ constexpr int brev(int i, int bits)
 }
 __host__ __device__ constexpr int fft_lanes(int nt) { return 1 << (ilog2c(nt) / 2); }
 __host__ __device__ constexpr int fft_rows_per_cta(int nt) { return fft_lanes(nt) == 4 ? 8 : 4; }
-// nTheta = 1024 runs its 4 rows on 8 warps (the tiles *_w8 below)
-__host__ __device__ constexpr bool fft_w8(int nt) { return nt == 1024; }
+// nTheta = 512 and 1024 run their 4 rows on 8 warps (the tiles *_w8 below)
+__host__ __device__ constexpr bool fft_w8(int nt) { return nt == 512 || nt == 1024; }
 __host__ __device__ constexpr int fft_threads(int nt)
 {
-    return fft_w8(nt) ? 2 * fft_rows_per_cta(nt) * fft_lanes(nt) : fft_rows_per_cta(nt) * fft_lanes(nt);
+    return fft_w8(nt) ? 8 * 32 : fft_rows_per_cta(nt) * fft_lanes(nt);
 }
 constexpr int FFT_MAX_THREADS = 256;  // fft_threads of every supported nTheta is at most this
 // Staging of R rows' mode columns: (mode index mi, row r2) at sidx(); the
@@ -530,32 +531,36 @@ __device__ __forceinline__ void row_fft(float2* a, float2* tb, int l, const floa
     for (int s = 0; s < S; s++) fft_regs<L, INV>(a + s * L);
 }
 
-// nTheta = 1024: the CTA's 4 rows on 8 warps.  All 8 share the input (the
-// divergence, half a row each), the unpacking (half the modes of a row
-// each) and the spectrum stores; the transform of each row runs on one warp
-// (row_fft) in between, the rows passing through shared memory behind the
-// transpose/staging region.  One warp per row for every phase left the 7 or
-// 8 rows an SM holds latency-bound from end to end.
-template <int MODE>
+// nTheta = 512 and 1024: the CTA's 4 rows on 8 warps.  All 8 share the
+// input (the divergence, half a row each, a row's points n = l + 32 r), the
+// unpacking (half the modes of a row each) and the spectrum stores; the
+// transform of each row runs on its L = fft_lanes(N) lanes (row_fft: one
+// warp per row at 1024, two rows per warp at 512) in between, the rows
+// passing through shared memory behind the transpose/staging region.  One
+// warp per row for every phase left the 7 or 8 rows an SM holds
+// latency-bound from end to end; at 512 the 4-row tiles had 2 warps.
+template <int MODE, int N>
 __device__ __forceinline__ void div_fft_tile_w8(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int blk,
                                                 int tid, float2* sm2)
 {
-    constexpr int N = 1024, P = 32, R = 4, LGR = 2, np = 2 * N, H = P / 2;
+    // NR registers of 32 lanes hold a row, H of them each of its 2 warps
+    constexpr int R = 4, LGR = 2, np = 2 * N, NR = N / 32, H = NR / 2;
+    constexpr int L = fft_lanes(N), P = N / L, S = P / L, LGL = ilog2c(L);
     const int w = tid >> 5, l = tid & 31, lr = w & 3, h = w >> 2;
     const int j0 = blk * R, j = j0 + lr;
     float2* zrow = sm2 + fft_region_len(N) + lr * N;  // this warp's row: z_n, then X_k
     {
-        // divergence of points n = l + 32 r, r in [16h, 16h + 16)
+        // divergence of points n = l + 32 r, r in [H h, H h + H)
         const float* __restrict__ src = MODE == 0 ? b.cu : b.u[uv_in];
         const float* __restrict__ vf = b.v[uv_in];
         float* __restrict__ uo = b.u[uv_out];
         float* __restrict__ vo = b.v[uv_out];
         const float fct = __ldg(b.divf + j), sN = __ldg(b.sinN + j), sS = __ldg(b.sinS + j);
         const size_t row = (size_t)j * np;
-        // c[q] holds register r = 16h + q - 1 (mod 32): the half plus one on each side
+        // c[q] holds register r = H h + q - 1 (mod NR): the half plus one on each side
         float2 c[H + 2];
 #pragma unroll
-        for (int q = 0; q < H + 2; q++) c[q] = ldg2(src + row + 2 * (l + 32 * ((16 * h + q - 1) & (P - 1))));
+        for (int q = 0; q < H + 2; q++) c[q] = ldg2(src + row + 2 * (l + 32 * ((H * h + q - 1) & (NR - 1))));
         const int wl = (l - 1) & 31, el = (l + 1) & 31;
         constexpr int CH = 8;
         const float2 zero = make_float2(0.0f, 0.0f);
@@ -564,7 +569,7 @@ __device__ __forceinline__ void div_fft_tile_w8(const KGeo& g, const KBufs& b, i
             float2 vA[CH], vB[CH], vC[CH];  // MODE 0: cv rows j-1, j, j+1; MODE 2: vf rows j-1, j
 #pragma unroll
             for (int qq = 0; qq < CH; qq++) {
-                const int i = 2 * (l + 32 * (16 * h + q0 + qq));
+                const int i = 2 * (l + 32 * (H * h + q0 + qq));
                 if (MODE == 0) {
                     vB[qq] = ldg2(b.cv + row + i);
                     vA[qq] = j > 0 ? ldg2(b.cv + row - np + i) : zero;
@@ -576,7 +581,7 @@ __device__ __forceinline__ void div_fft_tile_w8(const KGeo& g, const KBufs& b, i
             }
 #pragma unroll
             for (int qq = 0; qq < CH; qq++) {
-                const int q = q0 + qq, n = l + 32 * (16 * h + q), i = 2 * n;
+                const int q = q0 + qq, n = l + 32 * (H * h + q), i = 2 * n;
                 const float2 cc = c[q + 1];
                 // phi neighbours f_{2n-1}, f_{2n+2}: lane l -+ 1 of this register; for
                 // lane 0 (31) lane 31 (0) of the previous (next) register
@@ -627,21 +632,25 @@ __device__ __forceinline__ void div_fft_tile_w8(const KGeo& g, const KBufs& b, i
         }
     }
     __syncthreads();
-    if (h == 0) {  // the row's transform on one warp
+    if (tid < R * L) {  // the rows' transforms, L lanes each
+        const int tr = tid >> LGL, tl = tid & (L - 1);
+        float2* trow = sm2 + fft_region_len(N) + tr * N;
         float2 a[P];
 #pragma unroll
-        for (int r = 0; r < P; r++) a[r] = zrow[l + 32 * r];
-        row_fft<N, false>(a, sm2 + lr * fft_tblock(N), l, b.tw);
+        for (int r = 0; r < P; r++) a[r] = trow[tl + L * r];
+        row_fft<N, false>(a, sm2 + tr * fft_tblock(N), tl, b.tw);
 #pragma unroll
-        for (int k2 = 0; k2 < 32; k2++) zrow[l + 32 * k2] = a[brev(k2, 5)];  // X_{l + 32 k2}
+        for (int s2 = 0; s2 < S; s2++)
+#pragma unroll
+            for (int k2 = 0; k2 < L; k2++) trow[tl + L * s2 + P * k2] = a[s2 * L + brev(k2, LGL)];  // X_m
     }
     __syncthreads();  // every transpose block is read before the staging reuses the region
     {
-        // c_m = (1/nPhi)[E_m + e^{-i pi m/N} O_m], m = l + 32 k2, k2 in [16h, 16h + 16)
+        // c_m = (1/nPhi)[E_m + e^{-i pi m/N} O_m], m = l + 32 r, r in [H h, H h + H)
         const float scale = 1.0f / (float)np;
 #pragma unroll
         for (int q = 0; q < H; q++) {
-            const int m = l + 32 * (16 * h + q);
+            const int m = l + 32 * (H * h + q);
             const float2 za = zrow[m];
             float2 c;
             int mi;
@@ -679,7 +688,7 @@ __device__ __forceinline__ void div_fft_tile_n(const KGeo& g, const KBufs& b, in
                                                int tid, float2* sm2)
 {
     if constexpr (fft_w8(N)) {
-        if (tid < fft_threads(N)) div_fft_tile_w8<MODE>(g, b, uv_in, uv_out, blk, tid, sm2);
+        if (tid < fft_threads(N)) div_fft_tile_w8<MODE, N>(g, b, uv_in, uv_out, blk, tid, sm2);
         return;
     } else {
     constexpr int L = fft_lanes(N), P = N / L, S = P / L, R = fft_rows_per_cta(N);
@@ -1582,13 +1591,16 @@ inline SolveKernel solve_kernel(int nt)
 // spectrum, whose output is z_k = p_{2k} + i p_{2k+1}.  The solution is
 // mode-major (sol[(m-1)*nt + row]); the CTA first stages its R rows' columns
 // with the row index fastest.
-// nTheta = 1024 inverse on 8 warps: all 8 stage the solution columns, form
-// Y (half a row each) and update u (half a row each); the transform of each
-// row runs on one warp in between, the rows passing through shared memory.
+// nTheta = 512 and 1024 inverse on 8 warps: all 8 stage the solution
+// columns, form Y (half a row each) and update u (half a row each); the
+// transform of each row runs on its L lanes in between, the rows passing
+// through shared memory.
+template <int N>
 __device__ __forceinline__ void ifft_tile_w8(const KGeo& g, const KBufs& b, int uv_in, int uv_out, int blk, int tid,
                                              float2* sm2)
 {
-    constexpr int N = 1024, P = 32, R = 4, LGR = 2, np = 2 * N, H = P / 2, T = 8 * 32;
+    constexpr int R = 4, LGR = 2, np = 2 * N, NR = N / 32, H = NR / 2, T = 8 * 32;
+    constexpr int L = fft_lanes(N), P = N / L, S = P / L, LGL = ilog2c(L);
     const int w = tid >> 5, l = tid & 31, lr = w & 3, h = w >> 2;
     const int j0 = blk * R, j = j0 + lr;
     float2* zrow = sm2 + fft_region_len(N) + lr * N;  // this warp's row: Y_m, then z_k
@@ -1608,7 +1620,7 @@ __device__ __forceinline__ void ifft_tile_w8(const KGeo& g, const KBufs& b, int 
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < H; q++) {
-        const int m = l + 32 * (16 * h + q);
+        const int m = l + 32 * (H * h + q);
         if (m == 0) {
             const float un = sm2[sidx<R>(N - 1, lr)].x;  // X_nt = U_nt, real
             zrow[0] = make_float2(un, -un);
@@ -1622,13 +1634,17 @@ __device__ __forceinline__ void ifft_tile_w8(const KGeo& g, const KBufs& b, int 
         zrow[m] = make_float2(Er - Oi, Ei + Or);
     }
     __syncthreads();  // the staging is read before the transpose blocks reuse it
-    if (h == 0) {
+    if (tid < R * L) {  // the rows' transforms, L lanes each
+        const int tr = tid >> LGL, tl = tid & (L - 1);
+        float2* trow = sm2 + fft_region_len(N) + tr * N;
         float2 a[P];
 #pragma unroll
-        for (int r = 0; r < P; r++) a[r] = zrow[l + 32 * r];
-        row_fft<N, true>(a, sm2 + lr * fft_tblock(N), l, b.tw);
+        for (int r = 0; r < P; r++) a[r] = trow[tl + L * r];
+        row_fft<N, true>(a, sm2 + tr * fft_tblock(N), tl, b.tw);
 #pragma unroll
-        for (int k2 = 0; k2 < 32; k2++) zrow[l + 32 * k2] = a[brev(k2, 5)];  // z_{l + 32 k2}
+        for (int s2 = 0; s2 < S; s2++)
+#pragma unroll
+            for (int k2 = 0; k2 < L; k2++) trow[tl + L * s2 + P * k2] = a[s2 * L + brev(k2, LGL)];  // z_k
     }
     __syncthreads();
     const float* __restrict__ uf = b.u[uv_in];
@@ -1642,10 +1658,10 @@ __device__ __forceinline__ void ifft_tile_w8(const KGeo& g, const KBufs& b, int 
     for (int q0 = 0; q0 < H; q0 += CH) {
         float2 uu[CH];
 #pragma unroll
-        for (int qq = 0; qq < CH; qq++) uu[qq] = ldg2(uf + row + 2 * (l + 32 * (16 * h + q0 + qq)));
+        for (int qq = 0; qq < CH; qq++) uu[qq] = ldg2(uf + row + 2 * (l + 32 * (H * h + q0 + qq)));
 #pragma unroll
         for (int qq = 0; qq < CH; qq++) {
-            const int k = l + 32 * (16 * h + q0 + qq);
+            const int k = l + 32 * (H * h + q0 + qq);
             // p_{2k} = zc.x, p_{2k+1} = zc.y; the west neighbour p_{2k-1} = Im z_{k-1}
             const float2 zc = zrow[k];
             const float zpy = zrow[(k - 1) & (N - 1)].y;
@@ -1663,7 +1679,7 @@ __device__ __forceinline__ void ifft_tile_n(const KGeo& g, const KBufs& b, int u
                                             float2* sm2)
 {
     if constexpr (fft_w8(N)) {
-        if (tid < fft_threads(N)) ifft_tile_w8(g, b, uv_in, uv_out, blk, tid, sm2);
+        if (tid < fft_threads(N)) ifft_tile_w8<N>(g, b, uv_in, uv_out, blk, tid, sm2);
         return;
     } else {
     constexpr int L = fft_lanes(N), P = N / L, S = P / L, R = fft_rows_per_cta(N);
