@@ -1966,28 +1966,36 @@ inline cudaError_t flush_l2(void* buf, size_t bytes, int pattern, cudaStream_t s
 // A counting sort of the particles by the block of 4 rows x 32 columns of
 // cells they sit in: k_pkeys keys each particle and counts the blocks,
 // k_pscan turns the counts into offsets, k_pscatter lists the particles by
-// block.  Within a block the order is whatever the atomics give; the
-// result is a permutation either way.
+// block.  Both passes walk the particles in the visiting order of the
+// previous sort, in which a warp mostly holds particles of one or two
+// blocks, and issue one atomic per distinct block of the warp (lanes of a
+// block found with match.any), not one per particle: the atomics on a few
+// thousand counters were what the sort spent its time on.  Within a block the
+// order is whatever the atomics give; the result is a permutation either way.
 constexpr int PBLK_ROWS_LOG2 = 2, PBLK_COLS_LOG2 = 5;
 __host__ __device__ inline int pblocks(int nt)
 {
     return (nt >> PBLK_ROWS_LOG2) * ((2 * nt) >> PBLK_COLS_LOG2);
 }
 
-__global__ void __launch_bounds__(ELEM_THREADS) k_pkeys(KGeo g, const float2* __restrict__ part, int64_t n,
+// keys[t] = block of particle perm[t]; counts[block] += particles
+__global__ void __launch_bounds__(ELEM_THREADS) k_pkeys(KGeo g, const float2* __restrict__ part,
+                                                        const int* __restrict__ perm, int64_t n,
                                                         int* __restrict__ keys, int* __restrict__ counts)
 {
-    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const float2 p = __ldg(part + k);
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned act = __ballot_sync(0xffffffffu, t < n);
+    if (t >= n) return;
+    const float2 p = __ldg(part + __ldg(perm + t));
     // cell of (phi, theta), clamped: any position (even a non-finite one)
     // gets a valid block
     const float fr = p.y * g.invh, fc = p.x * g.invh;
     const int r = fr >= 0.0f ? (fr < (float)(g.nt - 1) ? (int)fr : g.nt - 1) : 0;
     const int c = fc >= 0.0f ? (fc < (float)g.mask ? (int)fc : g.mask) : 0;
     const int key = (r >> PBLK_ROWS_LOG2) * (g.np >> PBLK_COLS_LOG2) + (c >> PBLK_COLS_LOG2);
-    keys[k] = key;
-    atomicAdd(counts + key, 1);
+    keys[t] = key;
+    const unsigned same = __match_any_sync(act, key);
+    if ((int)(threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(counts + key, __popc(same));
 }
 
 // Exclusive prefix sum of counts[0 .. nb) in place, one CTA of 1024 threads.
@@ -2031,12 +2039,22 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_piota(int* __restrict__ perm, 
     if (k < n) perm[k] = (int)k;
 }
 
-__global__ void __launch_bounds__(ELEM_THREADS) k_pscatter(const int* __restrict__ keys, int64_t n,
-                                                           int* __restrict__ offsets, int* __restrict__ perm)
+// perm_out[offsets[key] + rank] = perm[t]: the warp's lanes of one block
+// take consecutive slots from one atomic
+__global__ void __launch_bounds__(ELEM_THREADS) k_pscatter(const int* __restrict__ keys,
+                                                           const int* __restrict__ perm, int64_t n,
+                                                           int* __restrict__ offsets, int* __restrict__ perm_out)
 {
-    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    perm[atomicAdd(offsets + keys[k], 1)] = (int)k;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned act = __ballot_sync(0xffffffffu, t < n);
+    if (t >= n) return;
+    const int key = __ldg(keys + t);
+    const unsigned same = __match_any_sync(act, key);
+    const int lane = threadIdx.x & 31, leader = __ffs(same) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(offsets + key, __popc(same));
+    base = __shfl_sync(same, base, leader);
+    perm_out[base + __popc(same & ((1u << lane) - 1u))] = __ldg(perm + t);
 }
 
 // ------------------------------------------------------------- probes

@@ -69,12 +69,15 @@ struct kamino_solver_s {
     // were set from outside
     int* pkeys = nullptr;
     int* pcounts = nullptr;
+    int* ptmp = nullptr;  // the new visiting order, copied into KBufs::pperm
     int64_t sorted_at = -1;  // step count of the last sort; -1: due
 };
 
 // Steps between rebuilds of the particles' visiting order: particles move
-// about a cell a step, so the order stays mostly block by block for a few.
-static const int kSortEvery = 8;
+// a fraction of a cell a step, so the order stays mostly block by block for
+// a few dozen (nTheta = 512, dt = 0.002: the advection launch takes the same
+// time with a rebuild every 8, 16 or 32 steps, and a rebuild ~25 us).
+static const int kSortEvery = 16;
 
 static const char* const kKernelNames[] = {"k_advect", "k_geo_centers", "k_div_fft",
                                            "k_solve",  "k_ifft_u",      "k_vgrad"};
@@ -307,9 +310,9 @@ extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
     const size_t rowf = align_up(sizeof(float) * nt), rowd = align_up(sizeof(double) * nt);
     const size_t tw = align_up(sizeof(float2) * nt), rt = align_up(sizeof(float2) * (nt + 1));
     const size_t s64 = align_up(sizeof(double) * kk::s64_stride(nt) * std::max(h->nfp64, 1));
-    const size_t pint = npart > 0 ? align_up(sizeof(int) * (size_t)npart) : 0;  // visiting order, sort keys
+    const size_t pint = npart > 0 ? align_up(sizeof(int) * (size_t)npart) : 0;  // visiting order, keys, new order
     const size_t pcnt = npart > 0 ? align_up(sizeof(int) * (size_t)kk::pblocks(nt)) : 0;
-    size_t total = 9 * field + 2 * spec + 2 * part + 13 * rowf + 4 * rowd + tw + rt + s64 + 2 * pint + pcnt;
+    size_t total = 9 * field + 2 * spec + 2 * part + 13 * rowf + 4 * rowd + tw + rt + s64 + 3 * pint + pcnt;
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&h->arena, total);
     if (e != cudaSuccess) {
@@ -360,6 +363,7 @@ extern "C" int kamino_create(const kamino_config* cfg, kamino_handle* out)
     if (npart > 0) {
         b.pperm = (const int*)take(pint);
         h->pkeys = (int*)take(pint);
+        h->ptmp = (int*)take(pint);
         h->pcounts = (int*)take(pcnt);
     } else {
         b.pperm = nullptr;
@@ -620,10 +624,13 @@ static int sort_particles(kamino_solver_s* h)
     const int nb = kk::pblocks(g.nt), T = kk::ELEM_THREADS;
     const unsigned blocks = (unsigned)((n + T - 1) / T);
     KCUDA(cudaMemsetAsync(h->pcounts, 0, sizeof(int) * (size_t)nb, h->stream));
-    kk::k_pkeys<<<blocks, T, 0, h->stream>>>(g, h->b.part[h->cur_r], n, h->pkeys, h->pcounts);
+    kk::k_pkeys<<<blocks, T, 0, h->stream>>>(g, h->b.part[h->cur_r], h->b.pperm, n, h->pkeys, h->pcounts);
     kk::k_pscan<<<1, 1024, 0, h->stream>>>(h->pcounts, nb);
-    kk::k_pscatter<<<blocks, T, 0, h->stream>>>(h->pkeys, n, h->pcounts, const_cast<int*>(h->b.pperm));
+    kk::k_pscatter<<<blocks, T, 0, h->stream>>>(h->pkeys, h->b.pperm, n, h->pcounts, h->ptmp);
     KCUDA(cudaGetLastError());
+    // into the buffer the step graphs read
+    KCUDA(cudaMemcpyAsync(const_cast<int*>(h->b.pperm), h->ptmp, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice,
+                          h->stream));
     h->sorted_at = h->steps;
     return KAMINO_OK;
 }
