@@ -150,12 +150,12 @@ def test_stages_commute_with_rotation_about_the_axis(kg, orc, nt, shift):
                     assert same, "%s after %s: %d values differ" % (k, stage, int((fb[k] != want).sum()))
 
 
-@pytest.mark.parametrize("nt,flags", [(64, 0), (64, 16), (1024, 0)])
+@pytest.mark.parametrize("nt,flags", [(64, 0), (64, 16), (512, 0), (1024, 0)])
 def test_stages_compose_to_step_bitwise(kg, orc, nt, flags):
     """advection(), geometric(), projection() called one by one (separate
     geometric, re-staggering and divergence kernels) give the bits of the
-    fused step; at nTheta = 1024 the step computes the geometric step inside
-    the forward transform's launch."""
+    fused step (at nTheta = 512 and 1024 both on the 8-warp transform
+    tiles)."""
     st = kg.make_initial_state(nt, lmax=8, seed=5, n_particles=4096)
     cfg = kg.default_config(n_theta=nt, radius=1.0, dt=0.005 if nt < 1024 else 0.001, n_particles=4096, flags=flags)
     with kg.KaminoSolver(config=cfg) as a, kg.KaminoSolver(config=cfg) as b:
