@@ -159,7 +159,7 @@ __device__ __forceinline__ float advect_point(const float* __restrict__ u, const
 // clear the operations are sample()'s own, so the value is the same.
 template <int KIND>
 __device__ __forceinline__ float sample_ref_try(const float* __restrict__ f, float phiRaw, float thetaRaw,
-                                            const KGeo& g, bool& bad)
+                                                const KGeo& g, bool& bad)
 {
     const float phi = (KIND == KIND_VPHI) ? __fadd_rn(phiRaw, g.halfh) : phiRaw;
     const float theta = (KIND == KIND_VTHETA) ? __fsub_rn(thetaRaw, g.h) : __fsub_rn(thetaRaw, g.halfh);
