@@ -104,10 +104,26 @@ def test_ref_index_bit_exact_vs_reference_validatecoord(orc, nt):
     assert np.array_equal(c, g["cells_%d" % nt])
 
 
+# Relative L2 bounds of the FP64 restatement against the reference's FP32
+# kernels, per stage and field (u_phi, u_theta, thickness), each a few times
+# what the fixtures show at nTheta = 32 and 64: the advection and the
+# projection agree to FP32 rounding (~1e-6); the geometric stage's u_phi
+# carries the reference's FP32 Cardano root, which cancels near the equator
+# (~1.7e-4), and so does every whole step; the geometric stage leaves the
+# thickness untouched (exactly equal).
+ORACLE_VS_REF_TOL = {
+    "advection": (5e-6, 5e-6, 1e-6),
+    "geometric": (5e-4, 5e-7, 0.0),
+    "projection": (5e-6, 5e-6, 0.0),
+    "step": (6e-4, 3e-4, 1e-5),
+}
+
+
 @pytest.mark.parametrize("nt", [32, 64])
 def test_fp64_oracle_vs_reference_kernels(orc, nt):
-    """The FP64 restatement against the reference's FP32 kernels: equal up to
-    the reference's own FP32 rounding (rel. L2 <= 1e-3 per field)."""
+    """The FP64 restatement against the reference's FP32 kernels, stage by
+    stage and after 1 and 3 steps, within the reference's own FP32 error
+    (ORACLE_VS_REF_TOL); particles within 1e-5 rad (p99)."""
     g = _golden("ref_step.npz")
     pre = "nt%d_" % nt
     nt_, dt, npart, seed = g[pre + "meta"]
@@ -117,20 +133,20 @@ def test_fp64_oracle_vs_reference_kernels(orc, nt):
         o.load(st)
         getattr(o, stage)()
         f = o.fields()
-        for k in ("u_phi", "u_theta", "thickness"):
+        for k, tol in zip(("u_phi", "u_theta", "thickness"), ORACLE_VS_REF_TOL[stage]):
             err = orc.rel_l2(g[pre + stage + "_" + k], f[k])
-            assert err <= 1e-3, (stage, k, err)
+            assert err <= tol, (stage, k, err, tol)
     for n in (1, 3):
         o = orc.Oracle(nt, 1.0, dt, 0, int(npart))
         o.load(st)
         o.step(n)
         f = o.fields()
-        for k in ("u_phi", "u_theta", "thickness"):
+        for k, tol in zip(("u_phi", "u_theta", "thickness"), ORACLE_VS_REF_TOL["step"]):
             err = orc.rel_l2(g[pre + "step%d_" % n + k], f[k])
-            assert err <= 1e-3, (n, k, err)
+            assert err <= tol, (n, k, err, tol)
         d = np.abs(g[pre + "step%d_particles" % n].astype(np.float64) - f["particles"])
         d[:, 0] = np.minimum(d[:, 0], 2 * np.pi - d[:, 0])
-        assert np.percentile(d, 99) < 1e-4, (n, np.percentile(d, 99))
+        assert np.percentile(d, 99) < 1e-5, (n, np.percentile(d, 99))
 
 
 def _py_fbm_init(nt, radius=1.0):
